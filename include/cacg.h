@@ -1,0 +1,253 @@
+/*
+ * cacg.h -- C ABI of libcacg.so, the GB300 (sm_103a) implementation of the
+ * sclc/cacg communication-avoiding Chebyshev-basis (block) CG hot path.
+ *
+ * Three layers, all extern "C", plain pointers and sizes:
+ *   1. Drop-in replacements for the reference solver entry points
+ *      (cbcg_v1, bcbcg_v1), same symbols, same by-value structs, same
+ *      semantics, for one rank's work on one GPU.
+ *   2. The extended solver API (cacg_solve*, cacg_matrix_*), with explicit
+ *      bounds / tolerance / precision / residual-replacement parameters and a
+ *      status code instead of exit().
+ *   3. Kernel-level entry points (cacg_k_*) on device pointers, one per hot
+ *      operation of the reference, used by the parity tests.
+ * Plus the serving loop (cacg_server_*) and the seeded input generators.
+ *
+ * Errors: every int-returning function returns CACG_OK (0) or a negative
+ * CACG_ERR_* code; nothing calls exit().  The drop-ins return void like the
+ * reference, and leave their status in cacg_last_status().
+ */
+#ifndef CACG_H
+#define CACG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "cacg_ref_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define CACG_OK 0
+#define CACG_NOT_CONVERGED 1 /* result valid, tolerance not reached in maxit */
+#define CACG_PENDING 2       /* server: request not finished yet */
+#define CACG_ERR_ARG (-1)
+#define CACG_ERR_OOM (-2)
+#define CACG_ERR_CUDA (-3)
+#define CACG_ERR_BREAKDOWN (-4) /* zero/non-finite pivot or NaN/Inf in the iteration */
+#define CACG_ERR_TIMEOUT (-5)   /* a bounded device-side wait ran out */
+#define CACG_ERR_UNSUPPORTED (-6)
+#define CACG_ERR_BUSY (-7)      /* server: admission refused (memory budget) */
+#define CACG_ERR_NODEV (-8)     /* no CUDA device */
+
+/* ----------------------------------------------------------------- enums */
+#define CACG_BOUNDS_GERSCHGORIN 0 /* reference behaviour, src/common.c:53 */
+#define CACG_BOUNDS_GIVEN 1       /* [lambda_min, lambda_max] from params */
+#define CACG_BOUNDS_LANCZOS 2     /* lanczos_steps-step Lanczos estimate */
+
+#define CACG_TOL_ABS_COL0 0 /* reference: ||R(:,0)|| < tol (src/bcbcgKernel.c:524) */
+#define CACG_TOL_REL_ALL 1  /* max_c ||b_c - A x_c|| / ||b_c|| <= tol (true residual) */
+
+#define CACG_FP64 0  /* plain FP64 everywhere */
+#define CACG_MIXED 1 /* FP32 basis/SpMM/updates, FP64 Gram accumulation, LU, X, R,
+                        FP64 residual replacement */
+
+#define CACG_GRAM_AUTO 0
+#define CACG_GRAM_FMA 1  /* FP64 FMA pipe */
+#define CACG_GRAM_DMMA 2 /* FP64 tensor core (mma.sync m8n8k4 f64) */
+
+#define CACG_VAL_F64 0
+#define CACG_VAL_F32 1
+
+/* generators (cacg_gen_*) */
+#define CACG_GEN_LAPLACE2D_5PT 1
+#define CACG_GEN_LAPLACE3D_7PT 2
+#define CACG_GEN_STENCIL3D_27PT 3
+#define CACG_GEN_VARCOEF2D_5PT 4
+#define CACG_RHS_UNIFORM 0
+#define CACG_RHS_NORMAL 1
+#define CACG_RHS_BETA25 2
+#define CACG_RHS_ONES 3
+
+/* --------------------------------------------------------------- structs */
+typedef struct cacg_csr {
+    int64_t n;              /* rows == columns */
+    int64_t nnz;
+    const int32_t *row_ptr; /* n + 1 */
+    const int32_t *col_idx; /* nnz, ascending within a row not required */
+    const double *val;      /* nnz */
+} cacg_csr;
+
+typedef struct cacg_params {
+    int32_t s;            /* basis length (s-step), >= 2 */
+    int32_t bounds_mode;  /* CACG_BOUNDS_* */
+    double lambda_min;    /* used with CACG_BOUNDS_GIVEN */
+    double lambda_max;
+    int32_t lanczos_steps; /* used with CACG_BOUNDS_LANCZOS (default 50) */
+    int32_t tol_mode;     /* CACG_TOL_* */
+    double tol;           /* absolute (ABS_COL0) or relative (REL_ALL) */
+    int32_t maxit;        /* outer iterations */
+    int32_t precision;    /* CACG_FP64 / CACG_MIXED */
+    int32_t rr_period;    /* MIXED: FP64 residual replacement every rr_period
+                             outer iterations (0: only when the recurrence
+                             residual says converged) */
+    int32_t gram_variant; /* CACG_GRAM_* */
+    uint64_t lanczos_seed;
+    void *stream;         /* cudaStream_t, NULL = the library's own stream */
+    int32_t use_graph;    /* capture the outer iteration in a CUDA graph */
+    int32_t reserved[7];
+} cacg_params;
+
+typedef struct cacg_result {
+    int32_t status;      /* CACG_OK / CACG_NOT_CONVERGED / CACG_ERR_* */
+    int32_t iterations;  /* outer iterations executed */
+    int32_t residual_replacements;
+    int32_t m;
+    double lambda_min;   /* Chebyshev interval actually used */
+    double lambda_max;
+    double recurrence_norm0; /* ||R(:,0)|| of the recurrence residual at exit */
+    double true_relres_max;  /* max_c ||b_c - A x_c|| / ||b_c|| (FP64) */
+    double *true_relres;     /* optional caller array of m entries */
+    double seconds;          /* solve time on the device (CUDA events) */
+    int64_t launches;        /* kernels launched by the solve */
+    int32_t reserved[6];
+} cacg_result;
+
+/* ------------------------------------------------- 1. drop-in (reference) */
+/* Replaces void cbcg_v1(csrType_local, denseType, denseType, long s,
+ * double epsilon, int myid, int numprocs), src/cbcgKernel.h:21.
+ * One rank only (numprocs must be 1); B/X local n x 1 row-major; X in/out;
+ * Gerschgorin bounds; stops when ||R(:,0)|| < epsilon or after 1000 outer
+ * iterations (src/cbcgKernel.c:2). */
+void cbcg_v1(csrType_local mat, denseType B, denseType X, long s, double epsilon,
+             int myid, int numprocs);
+/* Replaces void bcbcg_v1(...), src/bcbcgKernel.h:22.  Same contract with
+ * m = B.local_num_col right-hand sides and 100 outer iterations
+ * (src/bcbcgKernel.c:3). */
+void bcbcg_v1(csrType_local mat, denseType B, denseType X, long s, double epsilon,
+              int myid, int numprocs);
+/* Status of the calling thread's last drop-in call (they return void). */
+int cacg_last_status(void);
+/* Iterations / final ||R(:,0)|| of the calling thread's last drop-in call. */
+int cacg_last_iterations(void);
+/* Override the drop-ins' outer-iteration cap (0 restores 1000 / 100). */
+void cacg_set_dropin_maxit(int maxit);
+
+/* --------------------------------------------------- 2. extended solver API */
+void cacg_params_default(cacg_params *p);
+const char *cacg_status_string(int status);
+
+/* Host pointers in and out: copies A, B to the device, solves, copies X
+ * (initial guess in, solution out) back.  m right-hand sides, n x m row-major. */
+int cacg_solve(const cacg_csr *A, const double *B, double *X, int32_t m,
+               const cacg_params *p, cacg_result *res);
+
+/* A resident matrix (FP64 values, plus FP32 values when mixed is requested). */
+typedef struct cacg_matrix cacg_matrix;
+int cacg_matrix_create(const cacg_csr *A_host, int32_t want_fp32, cacg_matrix **out);
+int cacg_matrix_destroy(cacg_matrix *A);
+int64_t cacg_matrix_device_bytes(const cacg_matrix *A);
+/* Device pointers: B_dev, X_dev are n x m row-major doubles on the device. */
+int cacg_solve_device(cacg_matrix *A, const double *B_dev, double *X_dev, int32_t m,
+                      const cacg_params *p, cacg_result *res);
+/* Device bytes of solver state for (n, m, s, precision): the admission cost. */
+int64_t cacg_workspace_bytes(int64_t n, int32_t m, int32_t s, int32_t precision);
+
+/* ------------------------------------------------ 3. kernel entry points */
+/* All pointers are device pointers; stream may be NULL (legacy default
+ * stream).  Each call is asynchronous on that stream. */
+
+/* src/common.c:53-106 gerschgorin_v1: out[0] = min_i(d_i - sum|a_ij|),
+ * out[1] = max_i(d_i + sum|a_ij|) (max initialised to DBL_MIN as in the
+ * reference).  out is 2 device doubles. */
+int cacg_k_gerschgorin(int64_t n, const int32_t *row_ptr, const int32_t *col_idx,
+                       const double *val, double *out, void *stream);
+
+/* Fused CSR SpMM + three-term epilogue (src/BLAS3.c:20-155, 913-976, 978-994):
+ *   Y = ca * (A X) + cb * Z1 + cc * Z2        (Z1 / Z2 may be NULL)
+ * X, Y, Z1, Z2 are n x w row-major with the given row strides (elements).
+ * vtype selects double or float for val / X / Y / Z (CACG_VAL_*). */
+int cacg_k_spmm(int32_t vtype, int64_t n, const int32_t *row_ptr,
+                const int32_t *col_idx, const void *val, int32_t w, const void *X,
+                int64_t ldx, void *Y, int64_t ldy, const void *Z1, int64_t ldz1,
+                const void *Z2, int64_t ldz2, double ca, double cb, double cc,
+                void *stream);
+
+/* src/common.c:182-256 BCBCG_chebyshevPolynomialBasisGen (and :109-179 for
+ * m == 1): S (n x s*m, row stride lds) with S[:, 0:m] = R on entry already
+ * or copied from R when R != NULL; column block j = T_j. */
+int cacg_k_basis(int32_t vtype, int64_t n, const int32_t *row_ptr,
+                 const int32_t *col_idx, const void *val, const void *R, int32_t m,
+                 int32_t s, double alpha, double beta, void *S, int64_t lds,
+                 void *stream);
+
+/* src/BLAS3.c:699-758 distributedMatLTransposeMatRMul(_updated):
+ *   C (ka x (kb1 + kb2)) = L^T [R1 | R2]   accumulated in FP64.
+ * L (n x ka), R1 (n x kb1), R2 (n x kb2, may be NULL with kb2 == 0).
+ * vtype: inputs double (accumulate FP64) or float (FP64-accurate accumulation
+ * of FP32 products).  variant: CACG_GRAM_*.  C is row-major, ldc >= kb1+kb2. */
+int cacg_k_gram(int32_t vtype, int32_t variant, int64_t n, const void *L, int64_t ldl,
+                int32_t ka, const void *R1, int64_t ldr1, int32_t kb1, const void *R2,
+                int64_t ldr2, int32_t kb2, double *C, int32_t ldc, void *stream);
+
+/* src/BLAS3.c:794-825 + :579-612 fused: Q = S - Q * beta (in place on Q),
+ * Q, S n x k (strides ldq, lds), beta k x k FP64 row-major. */
+int cacg_k_qupdate(int32_t vtype, int64_t n, int32_t k, void *Q, int64_t ldq,
+                   const void *S, int64_t lds, const double *beta, void *stream);
+
+/* src/BLAS3.c:794-825 + :579-612 + src/MatrixOperations.c:110-142 fused:
+ *   X += Q alpha;  R -= AQ alpha;  S0 = R (cast to vtype, may be NULL);
+ *   norms[c] = ||R(:,c)||^2 for c < m (may be NULL).
+ * Q, AQ n x k (vtype, strides ldq), alpha k x m FP64, X, R n x m FP64. */
+int cacg_k_xrupdate(int32_t vtype, int64_t n, int32_t k, int32_t m, const void *Q,
+                    const void *AQ, int64_t ldq, const double *alpha, double *X,
+                    double *R, void *S0, int64_t lds, double *norms, void *stream);
+
+/* src/DLSsolvers.c:106-208 LUsolver_v1_KeeplhsMat: Y (k x r) = M^{-1} RHS by
+ * Crout LU without pivoting (U unit-diagonal).  status (device int, may be
+ * NULL) is set to 1 on a zero or non-finite pivot. */
+int cacg_k_lu(int32_t k, const double *M, int32_t r, const double *RHS, double *Y,
+              int *status, void *stream);
+
+/* Number of CUDA kernels this library has launched in this process. */
+int64_t cacg_launch_count(void);
+
+/* ----------------------------------------------------------- serving loop */
+typedef struct cacg_server cacg_server;
+typedef struct cacg_server_config {
+    int64_t mem_budget_bytes; /* device bytes admitted requests may hold */
+    int32_t max_active;       /* concurrent requests on the device */
+    int32_t reserved[7];
+} cacg_server_config;
+
+int cacg_server_create(const cacg_server_config *cfg, cacg_server **out);
+/* Enqueue one request: the server copies A, B (host) at admission; X_out
+ * (host, n x m) receives the solution.  Non-blocking; *ticket identifies it. */
+int cacg_server_submit(cacg_server *srv, const cacg_csr *A, const double *B,
+                       int32_t m, const cacg_params *p, double *X_out,
+                       int64_t *ticket);
+/* CACG_PENDING while running, else the request's final status; res filled. */
+int cacg_server_poll(cacg_server *srv, int64_t ticket, cacg_result *res);
+int cacg_server_wait(cacg_server *srv, int64_t ticket, cacg_result *res);
+/* Queue depth, active requests and device bytes in use. */
+int cacg_server_stats(cacg_server *srv, int64_t *queued, int64_t *active,
+                      int64_t *bytes_in_use);
+int cacg_server_destroy(cacg_server *srv);
+
+/* ------------------------------------------------------------ generators */
+int64_t cacg_gen_rows(int kind, int64_t N);
+int64_t cacg_gen_nnz(int kind, int64_t N);
+int cacg_gen_matrix(int kind, int64_t N, double shift, double sigma, uint64_t seed,
+                    int32_t *row_ptr, int32_t *col_idx, double *val);
+int cacg_gen_rhs(int dist, int64_t n, int m, uint64_t seed, double a, double b,
+                 double *out);
+double cacg_det_log(double x);
+double cacg_det_exp(double x);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CACG_H */
