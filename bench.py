@@ -1,0 +1,412 @@
+#!/usr/bin/env python3
+"""Benchmark: RHS solved per second to a 1e-8 true relative residual.
+
+Workload (default): block s-step Chebyshev CG on the 3-D 27-point stencil,
+128^3 grid (n = 2,097,152, nnz = 55,742,968; diagonal 26, off-diagonals -1,
+int32 CSR), 16 right-hand sides U[-1, 1) from seed 2, s = 6, Chebyshev interval
+[0.05, 52], FP64 residual replacement every 5 outer iterations, x0 = 0.
+One step = one complete solve of the 16-RHS block (all columns to true
+relative residual <= 1e-8), inputs resident in HBM.  The headline value is the
+mixed-precision mode; the plain FP64 mode is timed on the same inputs for the
+mixed-vs-FP64 ratio.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+N > 1 (torchrun): every rank solves its own replica (requests are independent;
+the path has no cross-GPU exchange), value = all ranks' RHS / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "RHS solved/s to 1e-8 rel. residual, mixed vs FP64; SpMM HBM GB/s; p99 latency"
+
+WORKLOADS = {
+    # the headline configuration (3-D 27-point 128^3, 16 RHS)
+    "st27_128_m16": dict(kind="st3d27", N=128, m=16, s=6, rhs="uniform", seed=2, a=-1.0,
+                         b=1.0, bounds=("given", 0.05, 52.0), rr=5, tol=1e-8),
+    # a small instance of the same family (for quick checks)
+    "st27_32_m16": dict(kind="st3d27", N=32, m=16, s=6, rhs="uniform", seed=2, a=-1.0,
+                        b=1.0, bounds=("given", 0.05, 52.0), rr=5, tol=1e-8),
+}
+CPU_SAMPLE_N = {"st27_128_m16": 48, "st27_32_m16": 16}
+
+
+def peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (read-only queries)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.out = io.StringIO()
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.write(line)
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        rows = list(csv.reader(io.StringIO(self.out.getvalue())))
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_inputs(w):
+    import cacg_gb300 as cg
+
+    rp, ci, v = cg.gen_matrix(w["kind"], w["N"])
+    n = len(rp) - 1
+    B = cg.gen_rhs(w["rhs"], n, w["m"], w["seed"], w["a"], w["b"])
+    return rp, ci, v, B
+
+
+def params(w, precision):
+    import cacg_gb300 as cg
+
+    return cg.Params(s=w["s"], bounds=w["bounds"], tol=w["tol"], maxit=1000,
+                     precision=precision, rr_period=w["rr"])
+
+
+# ------------------------------------------------------------ CPU baseline
+def reference_sample(wname, w, iters_full, cores):
+    """Time the reference solver (oracle/_ref, threaded MPI shim, `cores`
+    ranks) on the same stencil family at a reduced grid; extrapolate the
+    per-iteration time linearly in n (SpMM, Gram and update costs are all
+    linear in n at fixed m, s) to the full grid and multiply by the outer
+    iteration count the full problem needs.  Returns a dict."""
+    import numpy as np
+
+    import oracle as O
+
+    if not O.ref_available():
+        return None
+    Ns = CPU_SAMPLE_N.get(wname, 16)
+    rp, ci, v = O.gen_matrix(w["kind"], Ns)
+    n_s = len(rp) - 1
+    B = O.gen_rhs(w["rhs"], n_s, w["m"], w["seed"], w["a"], w["b"])
+    X0 = np.zeros_like(B)
+    lo, hi = w["bounds"][1], w["bounds"][2]
+    t1 = O.ref_solve(rp, ci, v, B, X0, w["s"], 0.0, (lo, hi), maxit=1, nranks=cores)[3]
+    t3 = O.ref_solve(rp, ci, v, B, X0, w["s"], 0.0, (lo, hi), maxit=3, nranks=cores)[3]
+    t_iter = max(t3 - t1, 1e-9) / 2.0
+    t_first = t1
+    n_full = O.port_lib().cacg_gen_rows(O.KINDS[w["kind"]], w["N"])
+    scale = n_full / n_s
+    t_solve = scale * (t_first + max(iters_full - 1, 0) * t_iter)
+    return {"value": w["m"] / t_solve, "unit": "RHS/s", "cores": cores, "kind": "reference",
+            "sample": ("reference bcbcg_v1 (src/bcbcgKernel.c) on the %s stencil at %d^3 "
+                       "(n=%d), %d MPI ranks as threads, 1 and 3 outer iterations timed "
+                       "(%.3f s, %.3f s); per-iteration time scaled by n_full/n_sample=%.1f "
+                       "and by %d outer iterations (the FP64 iteration count of the full "
+                       "problem): extrapolated" % (w["kind"], Ns, n_s, cores, t1, t3, scale,
+                                                   iters_full)),
+            "seconds_extrapolated": t_solve, "sample_seconds": t1 + t3}
+
+
+def run_reference_arm(args, w, rank):
+    if rank != 0:
+        return 0
+    import oracle as O
+
+    cores = os.cpu_count() or 1
+    if not O.ref_available():
+        print(json.dumps({"impl": "reference", "unavailable": "reference sources not built"}))
+        return 0
+    iters_full = int(os.environ.get("CACG_REF_ITERS", "0")) or ref_iteration_hint(args.workload)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = reference_sample(args.workload, w, iters_full, cores)
+        if i >= args.warmup:
+            vals.append(r)
+    v = statistics.median([r["value"] for r in vals])
+    ms = 1e3 * statistics.median([r["sample_seconds"] for r in vals])
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "RHS/s",
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": args.workload, **cfg_public(w)},
+           "cpu_baseline": {"value": v, "unit": "RHS/s", "cores": cores, "kind": "reference",
+                            "sample": vals[-1]["sample"]},
+           "e2e": {"value": v, "unit": "RHS/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def ref_iteration_hint(wname):
+    # outer iterations of the FP64 solve of the full problem, recorded by the
+    # GPU arm (profiles/bench_iterations.json); 1 if unknown
+    p = os.path.join(HERE, "profiles", "bench_iterations.json")
+    try:
+        with open(p) as f:
+            return int(json.load(f)[wname]["fp64_iterations"])
+    except Exception:
+        return 1
+
+
+def cfg_public(w):
+    return {"stencil": w["kind"], "grid": w["N"], "n": None, "rhs": w["m"], "s": w["s"],
+            "bounds": list(w["bounds"][1:]), "tol": w["tol"], "rr_period": w["rr"],
+            "x0": 0, "l2": "inputs larger than L2 (A alone > 129 MB)"}
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu_arm(args, w, rank, world):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import cacg_gb300 as cg
+    from cacg_gb300 import _lib as L
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    lib = cg.lib()
+    rp, ci, v, B = make_inputs(w)
+    n, m = B.shape
+    nnz = len(v)
+    M = cg.Matrix(rp, ci, v, want_fp32=True)
+    dB = torch.from_numpy(B).cuda()
+    dX = torch.zeros_like(dB)
+    pm = params(w, "mixed")
+    p64 = params(w, "fp64")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def solve(p):
+        dX.zero_()
+        return M.solve_device(dB.data_ptr(), dX.data_ptr(), m, p)
+
+    # warm-up
+    for _ in range(args.warmup):
+        info = solve(pm)
+    # timed mixed solves
+    lib.cacg_profile_reset()
+    lib.cacg_profile_enable(1)
+    clocks = ClockSampler(dev)
+    barrier()
+    clocks.start()
+    l0 = cg.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    infos = []
+    for _ in range(args.steps):
+        infos.append(solve(pm))
+    e1.record()
+    barrier()
+    launches = cg.launch_count() - l0
+    clk = clocks.stop()
+    lib.cacg_profile_enable(0)
+    ms_total = e0.elapsed_time(e1)
+    t = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * args.steps * m / (ms_max * 1e-3)
+    relres = max(i["true_relres_max"] for i in infos)
+    iters_mixed = infos[-1]["iterations"]
+    assert all(i["status"] == 0 for i in infos), [i["status"] for i in infos]
+    assert relres <= w["tol"], relres
+
+    # phases
+    phases = {}
+    for ph in range(8):
+        ms_, l_, b_, f_ = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
+        lib.cacg_profile_get(ph, C.byref(ms_), C.byref(l_), C.byref(b_), C.byref(f_))
+        if l_.value == 0:
+            continue
+        name = lib.cacg_profile_name(ph).decode()
+        phases[name] = {"ms": ms_.value, "launch_groups": None, "kernels": l_.value,
+                        "bytes": b_.value, "flops": f_.value}
+    for name, d in phases.items():
+        secs = d["ms"] * 1e-3
+        d["gbs"] = d["bytes"] / secs / 1e9 if secs > 0 else None
+        d["gflops"] = d["flops"] / secs / 1e9 if secs > 0 else None
+        d["share"] = d["ms"] / sum(x["ms"] for x in phases.values())
+
+    # FP64 mode on the same inputs (after the mixed warm-up the GPU is warm)
+    barrier()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record()
+    info64 = solve(p64)
+    f1.record()
+    barrier()
+    fp64_value = m / (f0.elapsed_time(f1) * 1e-3)
+    assert info64["status"] == 0 and info64["true_relres_max"] <= w["tol"]
+
+    # end to end through the C ABI with host buffers (cacg_solve): A, B and
+    # the initial X go host->device, X comes back, every step
+    Xh = np.zeros_like(B)
+    hb = 4 * (n + 1) + 12 * nnz + 2 * 8 * n * m
+    db = 8 * n * m
+    _X, _ = cg.solve(rp, ci, v, B, Xh, params=pm)  # warm-up
+    k_e2e = max(1, min(args.steps, 3))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        Xh = np.zeros_like(B)
+        Xe, ie = cg.solve(rp, ci, v, B, Xh, params=pm)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / k_e2e
+    assert ie["true_relres_max"] <= w["tol"]
+
+    out = None
+    if rank == 0:
+        hbm, bf16, src = peaks()
+        dom = max(phases.items(), key=lambda kv: kv[1]["ms"])
+        name, d = dom
+        per_launch_ms = d["ms"] / max(d["kernels"], 1)
+        bound = "tensor" if name == "gram" and d.get("tensor") else "hbm"
+        ach = d["gbs"]
+        spmm = phases.get("basis_spmm", {})
+        out = {
+            "metric": METRIC, "value": value, "unit": "RHS/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded generators)",
+            "config": {"workload": args.workload, **cfg_public(w), "n": n, "nnz": nnz,
+                       "precision": "mixed", "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "iterations_mixed": iters_mixed, "iterations_fp64": info64["iterations"],
+                       "true_relres_max": relres},
+            "fp64_value": fp64_value, "mixed_vs_fp64": value / world / fp64_value,
+            "spmm_hbm_gbs": spmm.get("gbs"),
+            "spmm_hbm_frac": (spmm.get("gbs") or 0) / hbm,
+            "roofline": {"kernel": name, "bound": bound, "achieved": ach,
+                         "peak": hbm if bound == "hbm" else bf16,
+                         "unit": "GB/s" if bound == "hbm" else "TFLOP/s",
+                         "frac": (ach or 0) / (hbm if bound == "hbm" else bf16),
+                         "peak_source": src, "traffic": traffic_for(name),
+                         "per_launch_ms": per_launch_ms,
+                         "algorithmic_bytes_per_launch": d["bytes"] / max(d["kernels"], 1)},
+            "phases": phases,
+            "e2e": {"value": m / e2e_s, "unit": "RHS/s", "h2d_bytes_per_step": hb,
+                    "d2h_bytes_per_step": db},
+            "clocks": clk, "gpu_launches": launches,
+        }
+        save_iterations(args.workload, info64["iterations"], iters_mixed)
+    M.close()
+    return out, info64["iterations"]
+
+
+def traffic_for(phase):
+    p = os.path.join(HERE, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(phase)
+    except Exception:
+        return None
+
+
+def save_iterations(wname, it64, itmx):
+    p = os.path.join(HERE, "profiles", "bench_iterations.json")
+    try:
+        d = {}
+        if os.path.exists(p):
+            with open(p) as f:
+                d = json.load(f)
+        d[wname] = {"fp64_iterations": it64, "mixed_iterations": itmx}
+        with open(p, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+            f.write("\n")
+    except Exception:
+        pass
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="st27_128_m16", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        return run_reference_arm(args, w, rank)
+    import torch
+
+    if world > 1:
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    out, it64 = run_gpu_arm(args, w, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            cb = reference_sample(args.workload, w, it64, os.cpu_count() or 1)
+            out["cpu_baseline"] = cb if cb else {"value": None, "unit": "RHS/s", "cores": 0,
+                                                 "kind": "reference",
+                                                 "sample": "reference unavailable"}
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,133 @@
+// cacg_internal.cuh -- shared device/host helpers of libcacg.so (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+
+#include "cacg.h"
+
+namespace cacg {
+
+// ---------------------------------------------------------------- status
+extern std::atomic<int64_t> g_launches;
+
+// device-side status bits (one int per solve, read by the host between steps)
+enum : int {
+    kStatusBreakdown = 1,  // zero / non-finite pivot in the small LU
+    kStatusNonFinite = 2,  // NaN/Inf in a residual norm
+};
+
+#define CACG_CUDA_TRY(expr)                                                  \
+    do {                                                                     \
+        cudaError_t _e = (expr);                                             \
+        if (_e != cudaSuccess) {                                             \
+            cacg::record_cuda_error(_e, #expr, __FILE__, __LINE__);          \
+            return _e == cudaErrorMemoryAllocation ? CACG_ERR_OOM : CACG_ERR_CUDA; \
+        }                                                                    \
+    } while (0)
+
+void record_cuda_error(cudaError_t e, const char *what, const char *file, int line);
+const char *last_cuda_error_text();
+
+inline int check_launch() {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        record_cuda_error(e, "kernel launch", __FILE__, __LINE__);
+        return CACG_ERR_CUDA;
+    }
+    return CACG_OK;
+}
+
+int sm_count();              // multiprocessors of the current device
+size_t max_smem_optin();     // opt-in shared memory per block (bytes)
+
+// ------------------------------------------------------- vector traits
+template <typename T> struct Vec16;
+template <> struct Vec16<double> {
+    using type = double2;
+    static constexpr int N = 2;
+};
+template <> struct Vec16<float> {
+    using type = float4;
+    static constexpr int N = 4;
+};
+
+__device__ __forceinline__ void vload(double (&d)[2], const double *p) {
+    double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+    d[0] = v.x; d[1] = v.y;
+}
+__device__ __forceinline__ void vload(float (&d)[4], const float *p) {
+    float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+    d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+}
+__device__ __forceinline__ void vstore(double *p, const double (&d)[2]) {
+    *reinterpret_cast<double2 *>(p) = make_double2(d[0], d[1]);
+}
+__device__ __forceinline__ void vstore(float *p, const float (&d)[4]) {
+    *reinterpret_cast<float4 *>(p) = make_float4(d[0], d[1], d[2], d[3]);
+}
+
+inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+// ------------------------------------------------- launcher declarations
+// All launchers return CACG_OK or CACG_ERR_*; they are asynchronous.
+
+// Y = ca*(A X) + cb*Z1 + cc*Z2, width w (T = double / float).
+template <typename T>
+int launch_spmm(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
+                const T *val, int w, const T *X, int64_t ldx, T *Y, int64_t ldy,
+                const T *Z1, int64_t ldz1, const T *Z2, int64_t ldz2, double ca,
+                double cb, double cc, double avg_nnz);
+
+// Residual in FP64 with optional cast copies:  R = B - A X ;  R32 = (float)R ;
+// S0 = (T)R ; norms[c] = ||R(:,c)||^2 (partials in ws, finished by a 2nd pass).
+int launch_residual(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
+                    const double *val, int m, const double *X, const double *B,
+                    double *R, void *S0, int s0_is_f32, int64_t lds, double *norms,
+                    double *ws, double avg_nnz);
+
+// Gram: C (ka x (kb1+kb2)) = L^T [R1 | R2] (FP64 accumulation).
+template <typename T>
+int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl, int ka,
+                const T *R1, int64_t ldr1, int kb1, const T *R2, int64_t ldr2, int kb2,
+                double *C1, int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes);
+size_t gram_workspace_bytes(int64_t n, int ka, int kb);
+
+// Q_out = S - Q_in * beta  (Q_out may alias S; never Q_in).
+template <typename T>
+int launch_qupdate(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo,
+                   const T *Qin, int64_t ldq, const T *S, int64_t lds, const double *beta);
+
+// X += Q alpha; R -= AQ alpha; S0 = (T)R; R32 = (float)R; norms.
+template <typename T>
+int launch_xrupdate(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,
+                    int64_t ldq, const double *alpha, double *X, double *R, T *S0,
+                    int64_t lds, float *R32, double *norms, double *ws);
+size_t norm_workspace_doubles(int64_t n, int m);
+
+// Small LU (Crout, U unit diagonal, no pivoting).
+int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *status);
+int launch_lu_solve(cudaStream_t st, int k, const double *F, int r, const double *RHS,
+                    double *Y);
+
+int launch_gerschgorin(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
+                       const double *val, double *out, double *ws);
+
+// norms[c] = ||R(:,c)||^2 of an n x m FP64 block (two-pass, fixed order).
+int launch_colnorm(cudaStream_t st, int64_t n, int m, const double *R, double *norms,
+                   double *ws);
+
+int launch_cast_f64_f32(cudaStream_t st, int64_t count, const double *in, float *out);
+int launch_cast_strided(cudaStream_t st, int64_t n, int w, const double *in, int64_t ldi,
+                        void *out, int out_is_f32, int64_t ldo);
+
+// Lanczos helpers (FP64): dot products with fixed-order reduction.
+int launch_dot(cudaStream_t st, int64_t n, const double *a, const double *b, double *out,
+               double *ws);
+int launch_axpby(cudaStream_t st, int64_t n, double a, const double *x, double b,
+                 double *y);
+
+}  // namespace cacg

@@ -1,0 +1,455 @@
+// k_gram.cu -- tall-skinny Gram products C = L^T [R1 | R2] with split-K.
+//
+// Reference operations replaced (sclc/cacg):
+//   distributedMatLTransposeMatRMul          src/BLAS3.c:699-726  Q^T AQ
+//   distributedMatLTransposeMatRMul_updated  src/BLAS3.c:730-758  (AQ)^T S, Q^T R
+// and the MPI_Allreduce(SUM) that follows each (src/BLAS3.c:721-722, 753-754):
+// on one GPU the cross-rank sum becomes the split-K reduction below.
+//
+// The K dimension is the row count n (millions), the output is k x (k+m)
+// (k = s*m <= 256).  Grid: blockIdx.x = split-K chunk of rows, blockIdx.y =
+// output tile (<= 128 x 128).  Each CTA stages KT-row slabs of L and R in
+// shared memory (cp.async, double-buffered) and every thread accumulates a
+// 4 x 4 micro-tile; partial tiles go to a workspace and a second kernel sums
+// them in a fixed chunk order, so the result is deterministic and depends only
+// on the problem's own shape (never on other work sharing the GPU).
+//
+// Accumulation:
+//   FP64 inputs  -- FP64 FMA (variant FMA) or FP64 tensor core mma.sync
+//                   m8n8k4 (variant DMMA);
+//   FP32 inputs  -- error-free products (p = a*b, e = fma(a,b,-p)) summed in
+//                   float-float with TwoSum, converted to FP64 per CTA chunk:
+//                   an FP64-accurate Gram of the FP32 basis without using the
+//                   FP64 pipe in the inner loop.
+#include <algorithm>
+
+#include "cacg_internal.cuh"
+
+namespace cacg {
+
+constexpr int kMA = 4, kMB = 4;  // micro-tile per thread
+constexpr int kMaxTile = 128;    // output tile edge
+
+template <typename T> struct GramKT;
+template <> struct GramKT<double> { static constexpr int value = 16; };
+template <> struct GramKT<float> { static constexpr int value = 32; };
+
+struct FF {  // float-float accumulator
+    float s, c;
+};
+
+__device__ __forceinline__ void acc_init(double &a) { a = 0.0; }
+__device__ __forceinline__ void acc_init(FF &a) { a.s = 0.f; a.c = 0.f; }
+__device__ __forceinline__ void acc_mac(double &acc, double l, double r) { acc = fma(l, r, acc); }
+__device__ __forceinline__ void acc_mac(FF &acc, float l, float r) {
+    float p = l * r;
+    float e = fmaf(l, r, -p);  // l*r == p + e exactly
+    float t = acc.s + p;       // TwoSum(acc.s, p)
+    float bp = t - acc.s;
+    float err = (acc.s - (t - bp)) + (p - bp);
+    acc.s = t;
+    acc.c += err + e;
+}
+__device__ __forceinline__ double acc_val(double a) { return a; }
+__device__ __forceinline__ double acc_val(FF a) { return (double)a.s + (double)a.c; }
+
+template <typename T> struct AccOf;
+template <> struct AccOf<double> { using type = double; };
+template <> struct AccOf<float> { using type = FF; };
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *g) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(g));
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *g) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(g));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+
+template <typename T>
+__device__ __forceinline__ void cp_elem(T *smem, const T *g) {
+    if constexpr (sizeof(T) == 8)
+        cp_async8(smem, g);
+    else
+        cp_async4(smem, g);
+}
+
+// Stage rows [r0, r0+KT) of the L tile (cols a0..a0+BA) and R tile into smem.
+template <typename T, int KT>
+__device__ __forceinline__ void stage_slab(T *Ls, T *Rs, int BA, int BB, int64_t r0,
+                                           int64_t rend, const T *L, int64_t ldl, int ka,
+                                           int a0, const T *R1, int64_t ldr1, int kb1,
+                                           const T *R2, int64_t ldr2, int kb2, int b0) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int idx = tid; idx < KT * BA; idx += nt) {
+        int r = idx / BA, a = idx % BA;
+        int64_t row = r0 + r;
+        T *dst = Ls + r * BA + a;
+        if (row < rend && a0 + a < ka)
+            cp_elem(dst, L + row * ldl + a0 + a);
+        else
+            *dst = T(0);
+    }
+    for (int idx = tid; idx < KT * BB; idx += nt) {
+        int r = idx / BB, b = idx % BB;
+        int64_t row = r0 + r;
+        int gb = b0 + b;
+        T *dst = Rs + r * BB + b;
+        if (row < rend && gb < kb1)
+            cp_elem(dst, R1 + row * ldr1 + gb);
+        else if (row < rend && gb - kb1 < kb2)
+            cp_elem(dst, R2 + row * ldr2 + (gb - kb1));
+        else
+            *dst = T(0);
+    }
+}
+
+constexpr int kGramMaxThreads = 768;
+
+template <typename T>
+__global__ void __launch_bounds__(kGramMaxThreads)
+    gram_fma_kernel(int64_t n, int64_t rows_per_chunk, const T *__restrict__ L, int64_t ldl,
+                    int ka, const T *__restrict__ R1, int64_t ldr1, int kb1,
+                    const T *__restrict__ R2, int64_t ldr2, int kb2, int BA, int BB,
+                    int tilesB, double *__restrict__ part) {
+    constexpr int KT = GramKT<T>::value;
+    using A = typename AccOf<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *Ls0 = reinterpret_cast<T *>(smem_raw);
+    T *Rs0 = Ls0 + KT * BA;
+    T *Ls1 = Rs0 + KT * BB;
+    T *Rs1 = Ls1 + KT * BA;
+
+    const int tile_a = blockIdx.y / tilesB, tile_b = blockIdx.y % tilesB;
+    const int a0 = tile_a * BA, b0 = tile_b * BB;
+    const int kb = kb1 + kb2;
+    const int nb = BB / kMB;
+    const int ta = threadIdx.x / nb, tb = threadIdx.x % nb;
+    const bool active = ta < BA / kMA;
+
+    const int64_t rbeg = (int64_t)blockIdx.x * rows_per_chunk;
+    const int64_t rend = min(n, rbeg + rows_per_chunk);
+
+    A acc[kMA][kMB];
+#pragma unroll
+    for (int i = 0; i < kMA; ++i)
+#pragma unroll
+        for (int j = 0; j < kMB; ++j) acc_init(acc[i][j]);
+
+    int64_t r0 = rbeg;
+    if (r0 < rend) {
+        stage_slab<T, KT>(Ls0, Rs0, BA, BB, r0, rend, L, ldl, ka, a0, R1, ldr1, kb1, R2, ldr2,
+                          kb2, b0);
+    }
+    cp_async_commit();
+    int buf = 0;
+    for (; r0 < rend; r0 += KT) {
+        T *Ls = buf ? Ls1 : Ls0;
+        T *Rs = buf ? Rs1 : Rs0;
+        if (r0 + KT < rend) {
+            stage_slab<T, KT>(buf ? Ls0 : Ls1, buf ? Rs0 : Rs1, BA, BB, r0 + KT, rend, L, ldl,
+                              ka, a0, R1, ldr1, kb1, R2, ldr2, kb2, b0);
+        }
+        cp_async_commit();
+        cp_async_wait_1();
+        __syncthreads();
+        if (active) {
+#pragma unroll 4
+            for (int r = 0; r < KT; ++r) {
+                T lv[kMA], rv[kMB];
+#pragma unroll
+                for (int i = 0; i < kMA; ++i) lv[i] = Ls[r * BA + ta * kMA + i];
+#pragma unroll
+                for (int j = 0; j < kMB; ++j) rv[j] = Rs[r * BB + tb * kMB + j];
+#pragma unroll
+                for (int i = 0; i < kMA; ++i)
+#pragma unroll
+                    for (int j = 0; j < kMB; ++j) acc_mac(acc[i][j], lv[i], rv[j]);
+            }
+        }
+        __syncthreads();
+        buf ^= 1;
+    }
+    cp_async_wait_all();
+    if (active) {
+        double *out = part + ((size_t)blockIdx.x * gridDim.y + blockIdx.y) * (size_t)BA * BB;
+#pragma unroll
+        for (int i = 0; i < kMA; ++i)
+#pragma unroll
+            for (int j = 0; j < kMB; ++j)
+                out[(ta * kMA + i) * BB + tb * kMB + j] = acc_val(acc[i][j]);
+    }
+    (void)kb;
+}
+
+// ------------------------------------------------------------ DMMA variant
+// FP64 tensor core: mma.sync.aligned.m8n8k4.row.col.f64.  A = L^T (8 x 4 per
+// step), B = R (4 x 8).  Each warp owns a list of 8x8 output tiles.
+constexpr int kDmmaMaxTilesPerWarp = 16;
+
+__global__ void __launch_bounds__(512)
+    gram_dmma_kernel(int64_t n, int64_t rows_per_chunk, const double *__restrict__ L,
+                     int64_t ldl, int ka, const double *__restrict__ R1, int64_t ldr1, int kb1,
+                     const double *__restrict__ R2, int64_t ldr2, int kb2, int BA, int BB,
+                     int tilesB, double *__restrict__ part) {
+    constexpr int KT = 16;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    // padded strides (BA + 4, BB + 4 with BA, BB multiples of 8) keep the
+    // 4-row x 8-column fragment reads free of bank conflicts
+    const int sa = BA + 4, sb = BB + 4;
+    double *Ls0 = reinterpret_cast<double *>(smem_raw);
+    double *Rs0 = Ls0 + KT * sa;
+    double *Ls1 = Rs0 + KT * sb;
+    double *Rs1 = Ls1 + KT * sa;
+
+    const int tile_a = blockIdx.y / tilesB, tile_b = blockIdx.y % tilesB;
+    const int a0 = tile_a * BA, b0 = tile_b * BB;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    const int ta8 = BA / 8, tb8 = BB / 8, ntiles = ta8 * tb8;
+    const int g = lane >> 2, t4 = lane & 3;
+
+    const int64_t rbeg = (int64_t)blockIdx.x * rows_per_chunk;
+    const int64_t rend = min(n, rbeg + rows_per_chunk);
+
+    double c[kDmmaMaxTilesPerWarp][2];
+#pragma unroll
+    for (int t = 0; t < kDmmaMaxTilesPerWarp; ++t) c[t][0] = c[t][1] = 0.0;
+
+    auto stage = [&](double *Ls, double *Rs, int64_t r0) {
+        for (int idx = threadIdx.x; idx < KT * BA; idx += blockDim.x) {
+            int r = idx / BA, a = idx % BA;
+            int64_t row = r0 + r;
+            double *dst = Ls + r * sa + a;
+            if (row < rend && a0 + a < ka)
+                cp_async8(dst, L + row * ldl + a0 + a);
+            else
+                *dst = 0.0;
+        }
+        for (int idx = threadIdx.x; idx < KT * BB; idx += blockDim.x) {
+            int r = idx / BB, b = idx % BB;
+            int64_t row = r0 + r;
+            int gb = b0 + b;
+            double *dst = Rs + r * sb + b;
+            if (row < rend && gb < kb1)
+                cp_async8(dst, R1 + row * ldr1 + gb);
+            else if (row < rend && gb - kb1 < kb2)
+                cp_async8(dst, R2 + row * ldr2 + (gb - kb1));
+            else
+                *dst = 0.0;
+        }
+    };
+
+    int64_t r0 = rbeg;
+    if (r0 < rend) stage(Ls0, Rs0, r0);
+    cp_async_commit();
+    int buf = 0;
+    for (; r0 < rend; r0 += KT) {
+        double *Ls = buf ? Ls1 : Ls0;
+        double *Rs = buf ? Rs1 : Rs0;
+        if (r0 + KT < rend) stage(buf ? Ls0 : Ls1, buf ? Rs0 : Rs1, r0 + KT);
+        cp_async_commit();
+        cp_async_wait_1();
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < KT; ks += 4) {
+#pragma unroll
+            for (int t = 0; t < kDmmaMaxTilesPerWarp; ++t) {
+                int tile = warp + t * nwarps;
+                if (tile < ntiles) {
+                    int ia = tile / tb8, ib = tile % tb8;
+                    double av = Ls[(ks + t4) * sa + ia * 8 + g];
+                    double bv = Rs[(ks + t4) * sb + ib * 8 + g];
+                    asm volatile(
+                        "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 "
+                        "{%0, %1}, {%2}, {%3}, {%0, %1};\n"
+                        : "+d"(c[t][0]), "+d"(c[t][1])
+                        : "d"(av), "d"(bv));
+                }
+            }
+        }
+        __syncthreads();
+        buf ^= 1;
+    }
+    cp_async_wait_all();
+    double *out = part + ((size_t)blockIdx.x * gridDim.y + blockIdx.y) * (size_t)BA * BB;
+#pragma unroll
+    for (int t = 0; t < kDmmaMaxTilesPerWarp; ++t) {
+        int tile = warp + t * nwarps;
+        if (tile < ntiles) {
+            int ia = tile / tb8, ib = tile % tb8;
+            out[(ia * 8 + g) * BB + ib * 8 + 2 * t4] = c[t][0];
+            out[(ia * 8 + g) * BB + ib * 8 + 2 * t4 + 1] = c[t][1];
+        }
+    }
+}
+
+// C[a][b] = sum over chunks p (in order) of part[p][tile(a,b)][a%BA][b%BB]
+__global__ void gram_reduce_kernel(const double *__restrict__ part, int nchunks, int ntiles,
+                                   int BA, int BB, int tilesB, int ka, int kb, int kb1,
+                                   double *__restrict__ C1, int ldc1, double *__restrict__ C2,
+                                   int ldc2) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ka * kb) return;
+    int a = idx / kb, b = idx % kb;
+    int tile = (a / BA) * tilesB + (b / BB);
+    size_t off = (size_t)tile * BA * BB + (size_t)(a % BA) * BB + (b % BB);
+    size_t stride = (size_t)ntiles * BA * BB;
+    double s = 0.0;
+    for (int p = 0; p < nchunks; ++p) s += part[off + (size_t)p * stride];
+    if (b < kb1)
+        C1[(size_t)a * ldc1 + b] = s;
+    else
+        C2[(size_t)a * ldc2 + (b - kb1)] = s;
+}
+
+struct GramPlan {
+    int BA, BB, tilesA, tilesB, nchunks;
+    int64_t rows_per_chunk;
+    size_t smem;
+    int threads;
+};
+
+static int round_up(int x, int q) { return (x + q - 1) / q * q; }
+
+template <typename T>
+static GramPlan plan_gram(int variant, int64_t n, int ka, int kb) {
+    GramPlan p;
+    const int q = (variant == CACG_GRAM_DMMA) ? 8 : 4;
+    p.BA = std::min(round_up(ka, q), kMaxTile);
+    // FMA variant: (BA/4) * (BB/4) threads, at most kGramMaxThreads
+    int maxBB = variant == CACG_GRAM_DMMA ? kMaxTile
+                                          : std::min(kMaxTile, (kGramMaxThreads * kMA * kMB / p.BA) / q * q);
+    p.BB = std::min(round_up(kb, q), maxBB);
+    p.tilesA = (ka + p.BA - 1) / p.BA;
+    p.tilesB = (kb + p.BB - 1) / p.BB;
+    int tiles = p.tilesA * p.tilesB;
+    int target = 2 * sm_count();
+    int64_t nchunks = (target + tiles - 1) / tiles;
+    const int KT = (variant == CACG_GRAM_DMMA) ? 16 : GramKT<T>::value;
+    int64_t maxchunks = std::max<int64_t>(1, (n + 4 * KT - 1) / (4 * KT));
+    if (nchunks > maxchunks) nchunks = maxchunks;
+    if (nchunks < 1) nchunks = 1;
+    p.rows_per_chunk = (n + nchunks - 1) / nchunks;
+    p.rows_per_chunk = (p.rows_per_chunk + KT - 1) / KT * KT;
+    p.nchunks = (int)((n + p.rows_per_chunk - 1) / p.rows_per_chunk);
+    if (p.nchunks < 1) p.nchunks = 1;
+    if (variant == CACG_GRAM_DMMA) {
+        int ntiles = (p.BA / 8) * (p.BB / 8);
+        int warps = (ntiles + kDmmaMaxTilesPerWarp - 1) / kDmmaMaxTilesPerWarp;
+        p.threads = 32 * std::max(1, std::min(16, warps));
+        p.smem = (size_t)2 * KT * ((p.BA + 4) + (p.BB + 4)) * sizeof(double);
+    } else {
+        p.threads = (p.BA / kMA) * (p.BB / kMB);
+        p.threads = round_up(p.threads, 32);
+        p.smem = (size_t)2 * KT * (p.BA + p.BB) * sizeof(T);
+    }
+    return p;
+}
+
+size_t gram_workspace_bytes(int64_t n, int ka, int kb) {
+    size_t best = 0;
+    for (int v = 1; v <= 2; ++v) {
+        GramPlan p = plan_gram<double>(v, n, ka, kb);
+        GramPlan q = plan_gram<float>(v, n, ka, kb);
+        size_t b1 = (size_t)p.nchunks * p.tilesA * p.tilesB * p.BA * p.BB * sizeof(double);
+        size_t b2 = (size_t)q.nchunks * q.tilesA * q.tilesB * q.BA * q.BB * sizeof(double);
+        best = std::max(best, std::max(b1, b2));
+    }
+    return best;
+}
+
+template <typename T>
+int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl, int ka,
+                const T *R1, int64_t ldr1, int kb1, const T *R2, int64_t ldr2, int kb2,
+                double *C1, int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes) {
+    const int kb = kb1 + kb2;
+    if (ka <= 0 || kb <= 0 || n < 0 || !C1 || (kb2 > 0 && !C2)) return CACG_ERR_ARG;
+    if (variant == CACG_GRAM_AUTO) variant = CACG_GRAM_FMA;
+    if (!std::is_same<T, double>::value) variant = CACG_GRAM_FMA;
+    if (variant == CACG_GRAM_DMMA) {
+        // each warp holds at most kDmmaMaxTilesPerWarp 8x8 tiles
+        int BA = std::min(round_up(ka, 8), kMaxTile), BB = std::min(round_up(kb, 8), kMaxTile);
+        if ((BA / 8) * (BB / 8) > 16 * kDmmaMaxTilesPerWarp) variant = CACG_GRAM_FMA;
+    }
+    GramPlan p = plan_gram<T>(variant, n, ka, kb);
+    size_t need = (size_t)p.nchunks * p.tilesA * p.tilesB * p.BA * p.BB * sizeof(double);
+    if (need > ws_bytes || !ws) return CACG_ERR_ARG;
+    dim3 grid(p.nchunks, p.tilesA * p.tilesB);
+    if (n > 0) {
+        if (variant == CACG_GRAM_DMMA) {
+            if constexpr (std::is_same<T, double>::value) {
+                static const bool attr = [] {
+                    cudaFuncSetAttribute(gram_dmma_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)max_smem_optin());
+                    return true;
+                }();
+                (void)attr;
+                gram_dmma_kernel<<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl,
+                                                                  ka, R1, ldr1, kb1, R2, ldr2,
+                                                                  kb2, p.BA, p.BB, p.tilesB,
+                                                                  ws);
+            }
+        } else {
+            static const bool attr = [] {
+                cudaFuncSetAttribute(gram_fma_kernel<T>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)max_smem_optin());
+                return true;
+            }();
+            (void)attr;
+            gram_fma_kernel<T><<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl,
+                                                                ka, R1, ldr1, kb1, R2, ldr2,
+                                                                kb2, p.BA, p.BB, p.tilesB, ws);
+        }
+        int rc = check_launch();
+        if (rc != CACG_OK) return rc;
+    } else {
+        cudaMemsetAsync(ws, 0, need, st);
+    }
+    int tot = ka * kb;
+    gram_reduce_kernel<<<(tot + 255) / 256, 256, 0, st>>>(ws, n > 0 ? p.nchunks : 1,
+                                                          p.tilesA * p.tilesB, p.BA, p.BB,
+                                                          p.tilesB, ka, kb, kb1, C1, ldc1,
+                                                          C2, ldc2);
+    return check_launch();
+}
+
+template int launch_gram<double>(cudaStream_t, int, int64_t, const double *, int64_t, int,
+                                 const double *, int64_t, int, const double *, int64_t, int,
+                                 double *, int, double *, int, double *, size_t);
+template int launch_gram<float>(cudaStream_t, int, int64_t, const float *, int64_t, int,
+                                const float *, int64_t, int, const float *, int64_t, int,
+                                double *, int, double *, int, double *, size_t);
+
+}  // namespace cacg
+
+using namespace cacg;
+
+extern "C" int cacg_k_gram(int32_t vtype, int32_t variant, int64_t n, const void *L,
+                           int64_t ldl, int32_t ka, const void *R1, int64_t ldr1, int32_t kb1,
+                           const void *R2, int64_t ldr2, int32_t kb2, double *C, int32_t ldc,
+                           void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (kb2 > 0 && !R2) return CACG_ERR_ARG;
+    size_t ws_bytes = gram_workspace_bytes(n, ka, kb1 + kb2);
+    double *ws = nullptr;
+    if (cudaMallocAsync((void **)&ws, ws_bytes, st) != cudaSuccess) return CACG_ERR_OOM;
+    int rc;
+    if (vtype == CACG_VAL_F64)
+        rc = launch_gram<double>(st, variant, n, (const double *)L, ldl, ka,
+                                 (const double *)R1, ldr1, kb1, (const double *)R2, ldr2, kb2,
+                                 C, ldc, C + kb1, ldc, ws, ws_bytes);
+    else if (vtype == CACG_VAL_F32)
+        rc = launch_gram<float>(st, variant, n, (const float *)L, ldl, ka, (const float *)R1,
+                                ldr1, kb1, (const float *)R2, ldr2, kb2, C, ldc, C + kb1, ldc, ws,
+                                ws_bytes);
+    else
+        rc = CACG_ERR_ARG;
+    cudaFreeAsync(ws, st);
+    return rc;
+}

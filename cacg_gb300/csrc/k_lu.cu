@@ -1,0 +1,148 @@
+// k_lu.cu -- the small dense solve of the CA iteration, in FP64.
+//
+// Reference operation replaced (sclc/cacg): LUsolver_v1_KeeplhsMat,
+// src/DLSsolvers.c:106-208 -- Crout LU with unit-diagonal U and NO pivoting
+// (reciprocal of the pivot times the pivot row, then the trailing update),
+// forward substitution dividing by L's diagonal through a reciprocal, back
+// substitution with U's unit diagonal.  The same elimination order is kept
+// so the GPU result matches the reference to rounding.
+//
+// The reference refactors Q^T AQ inside every call (twice per iteration:
+// for alpha, and one iteration later for beta); here the factor of each
+// Q^T AQ is computed once and reused by both solves.
+//
+// A zero or non-finite pivot sets *status = 1 (CACG_ERR_BREAKDOWN at the
+// host) instead of trapping; the arithmetic continues as the reference's
+// does (inf/NaN propagate) and the host stops the iteration.
+#include "cacg_internal.cuh"
+
+namespace cacg {
+
+constexpr int kLuThreads = 512;
+constexpr int kLuSmemK = 144;  // factor in shared memory up to k = 144 (162 KB)
+
+// One CTA.  W is the working matrix: shared memory when it fits, else F.
+__global__ void __launch_bounds__(kLuThreads)
+    lu_factor_kernel(int k, const double *__restrict__ M, double *__restrict__ F,
+                     int *__restrict__ status, int use_smem) {
+    extern __shared__ __align__(16) double Ws[];
+    double *W = use_smem ? Ws : F;
+    const int kk = k * k;
+    for (int i = threadIdx.x; i < kk; i += blockDim.x) W[i] = M[i];
+    __syncthreads();
+    int bad = 0;
+    for (int d = 0; d < k; ++d) {
+        const double piv = W[d * k + d];
+        if (threadIdx.x == 0 && (piv == 0.0 || !isfinite(piv))) bad = 1;
+        const double inv = 1.0 / piv;
+        for (int c = d + 1 + threadIdx.x; c < k; c += blockDim.x) W[d * k + c] *= inv;
+        __syncthreads();
+        const int t = k - d - 1;
+        for (int q = threadIdx.x; q < t * t; q += blockDim.x) {
+            int i = d + 1 + q / t, c = d + 1 + q % t;
+            W[i * k + c] = W[i * k + c] - W[i * k + d] * W[d * k + c];
+        }
+        __syncthreads();
+    }
+    if (use_smem)
+        for (int i = threadIdx.x; i < kk; i += blockDim.x) F[i] = W[i];
+    if (threadIdx.x == 0 && bad && status) atomicOr(status, kStatusBreakdown);
+}
+
+// Y (k x r) from the factor F and RHS (k x r).  Each CTA solves RC columns;
+// TPC threads cooperate on one column's inner products.
+constexpr int kLuRC = 32;
+constexpr int kLuTPC = 8;
+
+__global__ void __launch_bounds__(kLuRC * kLuTPC)
+    lu_solve_kernel(int k, const double *__restrict__ F, int r, const double *__restrict__ RHS,
+                    double *__restrict__ Y, int use_smem) {
+    extern __shared__ __align__(16) double sm[];
+    double *Fs = use_smem ? sm : nullptr;
+    double *Z = sm + (use_smem ? (size_t)k * k : 0);  // k x kLuRC
+    const double *Fm = use_smem ? Fs : F;
+    if (use_smem)
+        for (int i = threadIdx.x; i < k * k; i += blockDim.x) Fs[i] = F[i];
+    const int c0 = blockIdx.x * kLuRC;
+    const int cl = threadIdx.x / kLuTPC, sub = threadIdx.x % kLuTPC;
+    const int col = c0 + cl;
+    const bool active = col < r;
+    for (int i = threadIdx.x; i < k * kLuRC; i += blockDim.x) {
+        int row = i / kLuRC, cc = i % kLuRC;
+        Z[i] = (c0 + cc < r) ? RHS[(size_t)row * r + c0 + cc] : 0.0;
+    }
+    __syncthreads();
+    // forward: Z[i] = (Z[i] - sum_{q<i} L[i][q] Z[q]) * (1 / L[i][i])
+    for (int i = 0; i < k; ++i) {
+        double s = 0.0;
+        for (int q = sub; q < i; q += kLuTPC) s = fma(Fm[i * k + q], Z[q * kLuRC + cl], s);
+#pragma unroll
+        for (int o = kLuTPC / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kLuTPC);
+        if (sub == 0 && active) {
+            double inv = 1.0 / Fm[i * k + i];
+            Z[i * kLuRC + cl] = (Z[i * kLuRC + cl] - s) * inv;
+        }
+        __syncthreads();
+    }
+    // backward: Y[i] = Z[i] - sum_{q>i} U[i][q] Y[q]   (U unit diagonal)
+    for (int i = k - 2; i >= 0; --i) {
+        double s = 0.0;
+        for (int q = i + 1 + sub; q < k; q += kLuTPC) s = fma(Fm[i * k + q], Z[q * kLuRC + cl], s);
+#pragma unroll
+        for (int o = kLuTPC / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kLuTPC);
+        if (sub == 0 && active) Z[i * kLuRC + cl] = Z[i * kLuRC + cl] - s;
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < k * kLuRC; i += blockDim.x) {
+        int row = i / kLuRC, cc = i % kLuRC;
+        if (c0 + cc < r) Y[(size_t)row * r + c0 + cc] = Z[i];
+    }
+}
+
+int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *status) {
+    if (k <= 0) return CACG_ERR_ARG;
+    int use_smem = k <= kLuSmemK;
+    size_t smem = use_smem ? (size_t)k * k * sizeof(double) : 0;
+    static const bool attr = [] {
+        cudaFuncSetAttribute(lu_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    lu_factor_kernel<<<1, kLuThreads, smem, st>>>(k, M, F, status, use_smem);
+    return check_launch();
+}
+
+int launch_lu_solve(cudaStream_t st, int k, const double *F, int r, const double *RHS,
+                    double *Y) {
+    if (k <= 0 || r <= 0) return CACG_ERR_ARG;
+    size_t zbytes = (size_t)k * kLuRC * sizeof(double);
+    int use_smem = ((size_t)k * k * sizeof(double) + zbytes) <= max_smem_optin() - 1024;
+    size_t smem = zbytes + (use_smem ? (size_t)k * k * sizeof(double) : 0);
+    if (smem > max_smem_optin()) return CACG_ERR_UNSUPPORTED;
+    static const bool attr = [] {
+        cudaFuncSetAttribute(lu_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    int blocks = (r + kLuRC - 1) / kLuRC;
+    lu_solve_kernel<<<blocks, kLuRC * kLuTPC, smem, st>>>(k, F, r, RHS, Y, use_smem);
+    return check_launch();
+}
+
+}  // namespace cacg
+
+using namespace cacg;
+
+extern "C" int cacg_k_lu(int32_t k, const double *M, int32_t r, const double *RHS, double *Y,
+                         int *status, void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    double *F = nullptr;
+    if (cudaMallocAsync((void **)&F, (size_t)k * k * sizeof(double), st) != cudaSuccess)
+        return CACG_ERR_OOM;
+    int rc = launch_lu_factor(st, k, M, F, status);
+    if (rc == CACG_OK) rc = launch_lu_solve(st, k, F, r, RHS, Y);
+    cudaFreeAsync(F, st);
+    return rc;
+}

@@ -1,0 +1,545 @@
+// k_update.cu -- tall x small products with fused epilogues, norms,
+// Gerschgorin bounds, casts.
+//
+// Reference operations replaced (sclc/cacg):
+//   dense_distributedMatL_localMatR_Mul_v1  src/BLAS3.c:794-825  Q beta, Q alpha, AQ alpha
+//   dense_mat_mat_add_TP                    src/BLAS3.c:579-612  Q = S - Qbeta,
+//                                                                 X += Qalpha, R -= AQalpha
+//   norm2square_dist_denseMat_col_n         src/MatrixOperations.c:110-142 (+ Allreduce)
+//   gerschgorin_v1                          src/common.c:53-106 (+ Allreduce MIN/MAX)
+// The reference materialises Qbeta / Qalpha / AQalpha (n x k and n x m) and
+// then runs a separate axpby pass; here the product and the axpby are one
+// kernel, and the X/R update also writes the next basis block T_0 = R and the
+// per-column residual norms, so R is touched once per outer iteration.
+//
+// Reductions (norms, bounds, dots) are two-pass with a fixed grid and fixed
+// order, hence deterministic.
+#include <cfloat>
+
+#include "cacg_internal.cuh"
+
+namespace cacg {
+
+constexpr int kRowThreads = 256;
+constexpr int kRedBlocks = 304;  // fixed partial count for two-pass reductions
+
+// --------------------------------------------------------------- qupdate
+// Qout[i][c] = S[i][c] - sum_j Qin[i][j] * W[j][c] ; W = beta (k x k FP64),
+// staged in shared memory as T, in column blocks of BC.
+constexpr int kQuTR = 32;  // rows per tile
+constexpr int kQuM = 4;    // micro tile rows
+constexpr int kQuN = 4;    // micro tile cols
+
+template <typename T>
+__global__ void __launch_bounds__(512)
+    qupdate_kernel(int64_t n, int k, int BC, T *Qout, int64_t ldo, const T *__restrict__ Qin,
+                   int64_t ldq, const T *S, int64_t lds, const double *__restrict__ beta) {
+    // Qout may alias S (each element is read, then written, by one thread)
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *Ws = reinterpret_cast<T *>(smem_raw);  // k x BC
+    T *Qs = Ws + (size_t)k * BC;              // kQuTR x k
+    const int c0 = blockIdx.y * BC;
+    const int bc = min(BC, k - c0);
+    for (int idx = threadIdx.x; idx < k * BC; idx += blockDim.x) {
+        int j = idx / BC, c = idx % BC;
+        Ws[idx] = c < bc ? T(beta[(size_t)j * k + c0 + c]) : T(0);
+    }
+    const int nc = BC / kQuN;
+    const int tr = threadIdx.x / nc, tc = threadIdx.x % nc;
+    const bool active = tr < kQuTR / kQuM;
+    for (int64_t r0 = (int64_t)blockIdx.x * kQuTR; r0 < n; r0 += (int64_t)gridDim.x * kQuTR) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < kQuTR * k; idx += blockDim.x) {
+            int r = idx / k, j = idx % k;
+            int64_t row = r0 + r;
+            Qs[idx] = row < n ? Qin[row * ldq + j] : T(0);
+        }
+        __syncthreads();
+        if (active) {
+            T acc[kQuM][kQuN];
+#pragma unroll
+            for (int i = 0; i < kQuM; ++i)
+#pragma unroll
+                for (int q = 0; q < kQuN; ++q) acc[i][q] = T(0);
+            for (int j = 0; j < k; ++j) {
+                T qv[kQuM], wv[kQuN];
+#pragma unroll
+                for (int i = 0; i < kQuM; ++i) qv[i] = Qs[(tr * kQuM + i) * k + j];
+#pragma unroll
+                for (int q = 0; q < kQuN; ++q) wv[q] = Ws[j * BC + tc * kQuN + q];
+#pragma unroll
+                for (int i = 0; i < kQuM; ++i)
+#pragma unroll
+                    for (int q = 0; q < kQuN; ++q) acc[i][q] = fma(qv[i], wv[q], acc[i][q]);
+            }
+#pragma unroll
+            for (int i = 0; i < kQuM; ++i) {
+                int64_t row = r0 + tr * kQuM + i;
+                if (row >= n) continue;
+#pragma unroll
+                for (int q = 0; q < kQuN; ++q) {
+                    int c = tc * kQuN + q;
+                    if (c < bc) Qout[row * ldo + c0 + c] = S[row * lds + c0 + c] - acc[i][q];
+                }
+            }
+        }
+    }
+}
+
+template <typename T>
+int launch_qupdate(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo, const T *Qin,
+                   int64_t ldq, const T *S, int64_t lds, const double *beta) {
+    if (n <= 0) return CACG_OK;
+    if (k <= 0 || (const void *)Qout == (const void *)Qin) return CACG_ERR_ARG;
+    // column block: whole k when W and the Q tile fit comfortably
+    size_t budget = max_smem_optin() - 1024;
+    int BC = (k + kQuN - 1) / kQuN * kQuN;
+    while (BC > kQuN && ((size_t)k * BC + (size_t)kQuTR * k) * sizeof(T) > budget)
+        BC = (BC / 2 + kQuN - 1) / kQuN * kQuN;
+    if (((size_t)k * BC + (size_t)kQuTR * k) * sizeof(T) > budget) return CACG_ERR_UNSUPPORTED;
+    int threads = (kQuTR / kQuM) * (BC / kQuN);
+    threads = (threads + 31) / 32 * 32;
+    if (threads > 512) return CACG_ERR_UNSUPPORTED;
+    size_t smem = ((size_t)k * BC + (size_t)kQuTR * k) * sizeof(T);
+    static const bool attr = [] {
+        cudaFuncSetAttribute(qupdate_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    int64_t tiles = (n + kQuTR - 1) / kQuTR;
+    int64_t cap = (int64_t)sm_count() * 4;
+    dim3 grid((unsigned)(tiles < cap ? tiles : cap), (k + BC - 1) / BC);
+    qupdate_kernel<T><<<grid, threads, smem, st>>>(n, k, BC, Qout, ldo, Qin, ldq, S, lds, beta);
+    return check_launch();
+}
+
+template int launch_qupdate<double>(cudaStream_t, int64_t, int, double *, int64_t,
+                                    const double *, int64_t, const double *, int64_t,
+                                    const double *);
+template int launch_qupdate<float>(cudaStream_t, int64_t, int, float *, int64_t, const float *,
+                                   int64_t, const float *, int64_t, const double *);
+
+// -------------------------------------------------------------- xrupdate
+// One thread per (row, column c < m); a block covers XR_ROWS rows.  alpha is
+// staged in shared memory (FP64, or float-float hi/lo for FP32 inputs).
+struct FF2 {
+    float s, c;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kRowThreads)
+    xrupdate_kernel(int64_t n, int k, int m, int mp, const T *__restrict__ Q,
+                    const T *__restrict__ AQ, int64_t ldq, const double *__restrict__ alpha,
+                    double *__restrict__ X, double *__restrict__ R, T *__restrict__ S0,
+                    int64_t lds, float *__restrict__ R32, double *__restrict__ part) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int rows = blockDim.x / mp;
+    double *al = reinterpret_cast<double *>(smem_raw);  // k x m (FP64 path)
+    float *alh = reinterpret_cast<float *>(al + (size_t)k * m);  // k x m hi
+    float *all = alh + (size_t)k * m;                            // k x m lo
+    T *Qs = reinterpret_cast<T *>(all + (size_t)k * m + 4);      // rows x k
+    T *AQs = Qs + (size_t)rows * k;
+    double *red = reinterpret_cast<double *>(AQs + (size_t)rows * k + 4);  // rows x mp
+    // alignment fix-up for red
+    red = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(red) + 15) & ~uintptr_t(15));
+
+    for (int idx = threadIdx.x; idx < k * m; idx += blockDim.x) {
+        double a = alpha[idx];
+        al[idx] = a;
+        float h = (float)a;
+        alh[idx] = h;
+        all[idx] = (float)(a - (double)h);
+    }
+    const int r = threadIdx.x / mp, c = threadIdx.x % mp;
+    const bool active = r < rows && c < m;
+    double sq = 0.0;
+    for (int64_t r0 = (int64_t)blockIdx.x * rows; r0 < n; r0 += (int64_t)gridDim.x * rows) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < rows * k; idx += blockDim.x) {
+            int rr = idx / k, j = idx % k;
+            int64_t row = r0 + rr;
+            Qs[idx] = row < n ? Q[row * ldq + j] : T(0);
+            AQs[idx] = row < n ? AQ[row * ldq + j] : T(0);
+        }
+        __syncthreads();
+        const int64_t row = r0 + r;
+        if (active && row < n) {
+            double dx, dr;
+            if constexpr (sizeof(T) == 8) {
+                double ax = 0.0, ar = 0.0;
+                for (int j = 0; j < k; ++j) {
+                    double a = al[j * m + c];
+                    ax = fma((double)Qs[r * k + j], a, ax);
+                    ar = fma((double)AQs[r * k + j], a, ar);
+                }
+                dx = ax;
+                dr = ar;
+            } else {
+                // float-float: q * (ah + al) with the q*ah product split exactly
+                float sx = 0.f, cx = 0.f, sr = 0.f, cr = 0.f;
+                for (int j = 0; j < k; ++j) {
+                    float ah = alh[j * m + c], alo = all[j * m + c];
+                    float q = (float)Qs[r * k + j], aq = (float)AQs[r * k + j];
+                    float p = q * ah, e = fmaf(q, ah, -p);
+                    float t = sx + p, bp = t - sx;
+                    cx += ((sx - (t - bp)) + (p - bp)) + e + q * alo;
+                    sx = t;
+                    p = aq * ah;
+                    e = fmaf(aq, ah, -p);
+                    t = sr + p;
+                    bp = t - sr;
+                    cr += ((sr - (t - bp)) + (p - bp)) + e + aq * alo;
+                    sr = t;
+                }
+                dx = (double)sx + (double)cx;
+                dr = (double)sr + (double)cr;
+            }
+            double x = X[row * m + c] + dx;
+            double rv = R[row * m + c] - dr;
+            X[row * m + c] = x;
+            R[row * m + c] = rv;
+            if (S0) S0[row * lds + c] = (T)rv;
+            if (R32) R32[row * m + c] = (float)rv;
+            sq = fma(rv, rv, sq);
+        }
+    }
+    // block reduction of sq over rows, per column, fixed order
+    __syncthreads();
+    if (part) {
+        if (r < rows) red[r * mp + c] = (active ? sq : 0.0);
+        __syncthreads();
+        if (threadIdx.x < m) {
+            double s = 0.0;
+            for (int rr = 0; rr < rows; ++rr) s += red[rr * mp + threadIdx.x];
+            part[(size_t)blockIdx.x * m + threadIdx.x] = s;
+        }
+    }
+}
+
+// out[c] = sum over g < G of part[g*m + c]; non-finite -> status bit
+__global__ void colsum_kernel(const double *__restrict__ part, int G, int m,
+                              double *__restrict__ out) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m) return;
+    double s = 0.0;
+    for (int g = 0; g < G; ++g) s += part[(size_t)g * m + c];
+    out[c] = s;
+}
+
+size_t norm_workspace_doubles(int64_t n, int m) {
+    (void)n;
+    return (size_t)kRedBlocks * (size_t)(m > 0 ? m : 1);
+}
+
+static int pow2ceil(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+template <typename T>
+int launch_xrupdate(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,
+                    int64_t ldq, const double *alpha, double *X, double *R, T *S0, int64_t lds,
+                    float *R32, double *norms, double *ws) {
+    if (m <= 0 || k <= 0 || m > kRowThreads) return CACG_ERR_ARG;
+    if (norms && !ws) return CACG_ERR_ARG;
+    int mp = pow2ceil(m);
+    int rows = kRowThreads / mp;
+    size_t smem = (size_t)k * m * (8 + 4 + 4) + 16 + (size_t)2 * rows * k * sizeof(T) + 32 +
+                  (size_t)rows * mp * 8;
+    if (smem > max_smem_optin()) return CACG_ERR_UNSUPPORTED;
+    static const bool attr = [] {
+        cudaFuncSetAttribute(xrupdate_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    int G = kRedBlocks;
+    int64_t tiles = (n + rows - 1) / rows;
+    if (tiles < G) G = (int)(tiles > 0 ? tiles : 1);
+    xrupdate_kernel<T><<<G, kRowThreads, smem, st>>>(n, k, m, mp, Q, AQ, ldq, alpha, X, R, S0,
+                                                     lds, R32, norms ? ws : nullptr);
+    int rc = check_launch();
+    if (rc != CACG_OK || !norms) return rc;
+    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G, m, norms);
+    return check_launch();
+}
+
+template int launch_xrupdate<double>(cudaStream_t, int64_t, int, int, const double *,
+                                     const double *, int64_t, const double *, double *,
+                                     double *, double *, int64_t, float *, double *, double *);
+template int launch_xrupdate<float>(cudaStream_t, int64_t, int, int, const float *,
+                                    const float *, int64_t, const double *, double *, double *,
+                                    float *, int64_t, float *, double *, double *);
+
+// ------------------------------------------------------ residual epilogue
+// After R = B - A X (launch_spmm): S0 = cast(R), R32 = (float)R, norm partials.
+template <typename T>
+__global__ void __launch_bounds__(kRowThreads)
+    rowpost_kernel(int64_t n, int m, int mp, const double *__restrict__ R, T *__restrict__ S0,
+                   int64_t lds, float *__restrict__ R32, double *__restrict__ part) {
+    __shared__ double red[kRowThreads];
+    const int rows = blockDim.x / mp;
+    const int r = threadIdx.x / mp, c = threadIdx.x % mp;
+    const bool active = r < rows && c < m;
+    double sq = 0.0;
+    for (int64_t r0 = (int64_t)blockIdx.x * rows; r0 < n; r0 += (int64_t)gridDim.x * rows) {
+        int64_t row = r0 + r;
+        if (active && row < n) {
+            double v = R[row * m + c];
+            if (S0) S0[row * lds + c] = (T)v;
+            if (R32) R32[row * m + c] = (float)v;
+            sq = fma(v, v, sq);
+        }
+    }
+    red[threadIdx.x] = active ? sq : 0.0;
+    __syncthreads();
+    if (part && threadIdx.x < m) {
+        double s = 0.0;
+        for (int rr = 0; rr < rows; ++rr) s += red[rr * mp + threadIdx.x];
+        part[(size_t)blockIdx.x * m + threadIdx.x] = s;
+    }
+}
+
+int launch_residual(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
+                    const double *val, int m, const double *X, const double *B, double *R,
+                    void *S0, int s0_is_f32, int64_t lds, double *norms, double *ws,
+                    double avg_nnz) {
+    int rc = launch_spmm<double>(st, n, rp, ci, val, m, X, m, R, m, B, m, nullptr, 0, -1.0,
+                                 1.0, 0.0, avg_nnz);
+    if (rc != CACG_OK) return rc;
+    if (m > kRowThreads) return CACG_ERR_ARG;
+    int mp = pow2ceil(m);
+    int rows = kRowThreads / mp;
+    int G = kRedBlocks;
+    int64_t tiles = (n + rows - 1) / rows;
+    if (tiles < G) G = (int)(tiles > 0 ? tiles : 1);
+    if (s0_is_f32)
+        rowpost_kernel<float><<<G, kRowThreads, 0, st>>>(n, m, mp, R, (float *)S0, lds, nullptr,
+                                                         norms ? ws : nullptr);
+    else
+        rowpost_kernel<double><<<G, kRowThreads, 0, st>>>(n, m, mp, R, (double *)S0, lds,
+                                                          nullptr, norms ? ws : nullptr);
+    rc = check_launch();
+    if (rc != CACG_OK || !norms) return rc;
+    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G, m, norms);
+    return check_launch();
+}
+
+int launch_colnorm(cudaStream_t st, int64_t n, int m, const double *R, double *norms,
+                   double *ws) {
+    if (m > kRowThreads || m <= 0) return CACG_ERR_ARG;
+    int mp = pow2ceil(m);
+    int rows = kRowThreads / mp;
+    int G = kRedBlocks;
+    int64_t tiles = (n + rows - 1) / rows;
+    if (tiles < G) G = (int)(tiles > 0 ? tiles : 1);
+    rowpost_kernel<double><<<G, kRowThreads, 0, st>>>(n, m, mp, R, nullptr, 0, nullptr, ws);
+    int rc = check_launch();
+    if (rc != CACG_OK) return rc;
+    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G, m, norms);
+    return check_launch();
+}
+
+// ------------------------------------------------------------ Gerschgorin
+__global__ void __launch_bounds__(kRowThreads)
+    gersch_kernel(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                  const double *__restrict__ v, double *__restrict__ part) {
+    __shared__ double smin[kRowThreads], smax[kRowThreads];
+    double lmin = DBL_MAX, lmax = DBL_MIN;  // reference initial values
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0, diag = 0.0;
+        for (int p = rp[i]; p < rp[i + 1]; ++p) {
+            double a = v[p];
+            if ((int64_t)ci[p] != i)
+                acc += fabs(a);
+            else
+                diag = a;
+        }
+        lmax = fmax(lmax, acc + diag);
+        lmin = fmin(lmin, diag - acc);
+    }
+    smin[threadIdx.x] = lmin;
+    smax[threadIdx.x] = lmax;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = smin[0];
+        part[2 * blockIdx.x + 1] = smax[0];
+    }
+}
+
+__global__ void gersch_final_kernel(const double *__restrict__ part, int G,
+                                    double *__restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double lmin = DBL_MAX, lmax = DBL_MIN;
+    for (int g = 0; g < G; ++g) {
+        lmin = fmin(lmin, part[2 * g]);
+        lmax = fmax(lmax, part[2 * g + 1]);
+    }
+    out[0] = lmin;
+    out[1] = lmax;
+}
+
+int launch_gerschgorin(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
+                       const double *val, double *out, double *ws) {
+    int G = kRedBlocks;
+    int64_t need = (n + kRowThreads - 1) / kRowThreads;
+    if (need < G) G = (int)(need > 0 ? need : 1);
+    gersch_kernel<<<G, kRowThreads, 0, st>>>(n, rp, ci, val, ws);
+    int rc = check_launch();
+    if (rc != CACG_OK) return rc;
+    gersch_final_kernel<<<1, 32, 0, st>>>(ws, G, out);
+    return check_launch();
+}
+
+// ------------------------------------------------------------------ casts
+__global__ void cast_kernel(int64_t count, const double *__restrict__ in, float *__restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+int launch_cast_f64_f32(cudaStream_t st, int64_t count, const double *in, float *out) {
+    if (count <= 0) return CACG_OK;
+    int64_t blocks = (count + 255) / 256;
+    int64_t cap = (int64_t)sm_count() * 8;
+    cast_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(count, in, out);
+    return check_launch();
+}
+
+template <typename T>
+__global__ void cast_strided_kernel(int64_t n, int w, const double *__restrict__ in, int64_t ldi,
+                                    T *__restrict__ out, int64_t ldo) {
+    int64_t tot = n * w;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = q / w;
+        int c = (int)(q % w);
+        out[i * ldo + c] = (T)in[i * ldi + c];
+    }
+}
+
+int launch_cast_strided(cudaStream_t st, int64_t n, int w, const double *in, int64_t ldi,
+                        void *out, int out_is_f32, int64_t ldo) {
+    if (n <= 0) return CACG_OK;
+    int64_t blocks = (n * w + 255) / 256;
+    int64_t cap = (int64_t)sm_count() * 8;
+    unsigned g = (unsigned)(blocks < cap ? blocks : cap);
+    if (out_is_f32)
+        cast_strided_kernel<float><<<g, 256, 0, st>>>(n, w, in, ldi, (float *)out, ldo);
+    else
+        cast_strided_kernel<double><<<g, 256, 0, st>>>(n, w, in, ldi, (double *)out, ldo);
+    return check_launch();
+}
+
+// ----------------------------------------------------------- dot / axpby
+__global__ void __launch_bounds__(kRowThreads)
+    dot_kernel(int64_t n, const double *__restrict__ a, const double *__restrict__ b,
+               double *__restrict__ part) {
+    __shared__ double red[kRowThreads];
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(a[i], b[i], s);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+int launch_dot(cudaStream_t st, int64_t n, const double *a, const double *b, double *out,
+               double *ws) {
+    int G = kRedBlocks;
+    int64_t need = (n + kRowThreads - 1) / kRowThreads;
+    if (need < G) G = (int)(need > 0 ? need : 1);
+    dot_kernel<<<G, kRowThreads, 0, st>>>(n, a, b, ws);
+    int rc = check_launch();
+    if (rc != CACG_OK) return rc;
+    colsum_kernel<<<1, 32, 0, st>>>(ws, G, 1, out);
+    return check_launch();
+}
+
+__global__ void axpby_kernel(int64_t n, double a, const double *__restrict__ x, double b,
+                             double *__restrict__ y) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = a * x[i] + b * y[i];
+}
+
+int launch_axpby(cudaStream_t st, int64_t n, double a, const double *x, double b, double *y) {
+    if (n <= 0) return CACG_OK;
+    int64_t blocks = (n + 255) / 256;
+    int64_t cap = (int64_t)sm_count() * 8;
+    axpby_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(n, a, x, b, y);
+    return check_launch();
+}
+
+}  // namespace cacg
+
+using namespace cacg;
+
+extern "C" int cacg_k_gerschgorin(int64_t n, const int32_t *row_ptr, const int32_t *col_idx,
+                                  const double *val, double *out, void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    double *ws = nullptr;
+    if (cudaMallocAsync((void **)&ws, 2 * kRedBlocks * sizeof(double), st) != cudaSuccess)
+        return CACG_ERR_OOM;
+    int rc = launch_gerschgorin(st, n, row_ptr, col_idx, val, out, ws);
+    cudaFreeAsync(ws, st);
+    return rc;
+}
+
+extern "C" int cacg_k_qupdate(int32_t vtype, int64_t n, int32_t k, void *Q, int64_t ldq,
+                              const void *S, int64_t lds, const double *beta, void *stream) {
+    // in place on Q: the product reads all of Q's row, so stage a copy first
+    cudaStream_t st = (cudaStream_t)stream;
+    size_t es = vtype == CACG_VAL_F64 ? 8 : 4;
+    void *Qin = nullptr;
+    size_t bytes = (size_t)n * ldq * es;
+    if (cudaMallocAsync(&Qin, bytes > 0 ? bytes : 16, st) != cudaSuccess) return CACG_ERR_OOM;
+    cudaMemcpyAsync(Qin, Q, bytes, cudaMemcpyDeviceToDevice, st);
+    int rc;
+    if (vtype == CACG_VAL_F64)
+        rc = launch_qupdate<double>(st, n, k, (double *)Q, ldq, (const double *)Qin, ldq,
+                                    (const double *)S, lds, beta);
+    else if (vtype == CACG_VAL_F32)
+        rc = launch_qupdate<float>(st, n, k, (float *)Q, ldq, (const float *)Qin, ldq,
+                                   (const float *)S, lds, beta);
+    else
+        rc = CACG_ERR_ARG;
+    cudaFreeAsync(Qin, st);
+    return rc;
+}
+
+extern "C" int cacg_k_xrupdate(int32_t vtype, int64_t n, int32_t k, int32_t m, const void *Q,
+                               const void *AQ, int64_t ldq, const double *alpha, double *X,
+                               double *R, void *S0, int64_t lds, double *norms, void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    double *ws = nullptr;
+    if (cudaMallocAsync((void **)&ws, norm_workspace_doubles(n, m) * sizeof(double), st) !=
+        cudaSuccess)
+        return CACG_ERR_OOM;
+    int rc;
+    if (vtype == CACG_VAL_F64)
+        rc = launch_xrupdate<double>(st, n, k, m, (const double *)Q, (const double *)AQ, ldq,
+                                     alpha, X, R, (double *)S0, lds, nullptr, norms, ws);
+    else if (vtype == CACG_VAL_F32)
+        rc = launch_xrupdate<float>(st, n, k, m, (const float *)Q, (const float *)AQ, ldq, alpha,
+                                    X, R, (float *)S0, lds, nullptr, norms, ws);
+    else
+        rc = CACG_ERR_ARG;
+    cudaFreeAsync(ws, st);
+    return rc;
+}

@@ -214,6 +214,25 @@ int cacg_k_lu(int32_t k, const double *M, int32_t r, const double *RHS, double *
 /* Number of CUDA kernels this library has launched in this process. */
 int64_t cacg_launch_count(void);
 
+/* ------------------------------------------------------- phase profiling */
+/* The GPU counterpart of the reference's TIME_MEASURE_BCBCG_* phase timers
+ * (src/bcbcgKernel.c:19-24, 454-522): when enabled, every solve records CUDA
+ * events around each phase's kernels on the solve's stream and accumulates
+ * device time, launches, and the phase's algorithmic bytes and flops. */
+#define CACG_PHASE_BASIS 0    /* Chebyshev-step SpMM (width m) */
+#define CACG_PHASE_AQ 1       /* AQ = A Q SpMM (width k) */
+#define CACG_PHASE_GRAM 2     /* Q^T [AQ | R], (AQ)^T S */
+#define CACG_PHASE_QUPDATE 3  /* Q = S - Q beta */
+#define CACG_PHASE_XRUPDATE 4 /* X += Q alpha, R -= AQ alpha, norms */
+#define CACG_PHASE_LU 5       /* factor + solves */
+#define CACG_PHASE_RESIDUAL 6 /* R = B - A X (start, replacement, final) */
+#define CACG_PHASE_BOUNDS 7   /* Gerschgorin / Lanczos */
+#define CACG_NUM_PHASES 8
+void cacg_profile_enable(int on);
+void cacg_profile_reset(void);
+int cacg_profile_get(int phase, double *ms, int64_t *launches, double *bytes, double *flops);
+const char *cacg_profile_name(int phase);
+
 /* ----------------------------------------------------------- serving loop */
 typedef struct cacg_server cacg_server;
 typedef struct cacg_server_config {

@@ -1,0 +1,213 @@
+"""Kernel-level parity: each libcacg.so kernel (called through its C ABI entry
+point) against the oracle's restatement of the reference routine on the same
+seeded inputs.
+
+Tolerances (FP64 kernels differ from the reference only in summation order and
+fused multiply-add): normwise relative error <= 1e-12.  FP32 kernels are
+compared with the FP64 evaluation of the same FP32 inputs: <= 2e-6.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from gpu_util import dev, host, ptr, relerr
+
+pytestmark = pytest.mark.gpu
+
+F64, F32 = 0, 1
+
+
+def _mat(kind="st3d27", N=10, **kw):
+    return O.gen_matrix(kind, N, **kw)
+
+
+@pytest.mark.parametrize("kind,N", [("lap2d", 40), ("lap3d7", 12), ("st3d27", 10),
+                                    ("varcoef2d", 30)])
+@pytest.mark.parametrize("w", [1, 2, 3, 8, 16, 24, 32, 96, 130])
+def test_spmm_f64_matches_reference(lib, torch_cuda, kind, N, w):
+    torch = torch_cuda
+    rp, ci, v = _mat(kind, N, shift=1e-6, sigma=1.5, seed=3)
+    n = len(rp) - 1
+    X = O.gen_rhs("normal", n, w, 7)
+    Z1 = O.gen_rhs("normal", n, w, 8)
+    Z2 = O.gen_rhs("normal", n, w, 9)
+    want_plain = O.ref_spmm(rp, ci, v, X) if O.ref_available() else O.port_spmm(rp, ci, v, X)
+    ca, cb, cc = 0.7, -1.3, -1.0
+    want = ca * want_plain + cb * Z1 + cc * Z2
+    d = {k: dev(torch, a) for k, a in dict(rp=rp, ci=ci, v=v, X=X, Z1=Z1, Z2=Z2).items()}
+    Y = torch.empty((n, w), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_spmm(F64, n, ptr(d["rp"]), ptr(d["ci"]), ptr(d["v"]), w, ptr(d["X"]), w,
+                         ptr(Y), w, ptr(d["Z1"]), w, ptr(d["Z2"]), w, ca, cb, cc, None)
+    assert rc == 0
+    assert relerr(host(Y), want) <= 1e-13
+    Y0 = torch.empty((n, w), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_spmm(F64, n, ptr(d["rp"]), ptr(d["ci"]), ptr(d["v"]), w, ptr(d["X"]), w,
+                         ptr(Y0), w, None, 0, None, 0, 1.0, 0.0, 0.0, None)
+    assert rc == 0
+    assert relerr(host(Y0), want_plain) <= 1e-13
+
+
+@pytest.mark.parametrize("w", [1, 4, 5, 16, 32, 96])
+def test_spmm_f32(lib, torch_cuda, w):
+    torch = torch_cuda
+    rp, ci, v = _mat("st3d27", 12)
+    n = len(rp) - 1
+    X = O.gen_rhs("uniform", n, w, 3, -1.0, 1.0).astype(np.float32)
+    v32 = v.astype(np.float32)
+    want = O.port_spmm(rp, ci, v32.astype(np.float64), X.astype(np.float64))
+    d = {k: dev(torch, a) for k, a in dict(rp=rp, ci=ci, v=v32, X=X).items()}
+    Y = torch.empty((n, w), dtype=torch.float32, device="cuda")
+    rc = lib.cacg_k_spmm(F32, n, ptr(d["rp"]), ptr(d["ci"]), ptr(d["v"]), w, ptr(d["X"]), w,
+                         ptr(Y), w, None, 0, None, 0, 1.0, 0.0, 0.0, None)
+    assert rc == 0
+    assert relerr(host(Y), want) <= 2e-6
+
+
+@pytest.mark.parametrize("kind,N,m,s", [("lap2d", 48, 1, 4), ("lap3d7", 12, 8, 8),
+                                        ("st3d27", 10, 16, 6), ("lap3d7", 10, 3, 5)])
+def test_basis_matches_reference(lib, torch_cuda, kind, N, m, s):
+    torch = torch_cuda
+    rp, ci, v = _mat(kind, N)
+    n = len(rp) - 1
+    R = O.gen_rhs("normal", n, m, 11)
+    lo, hi = O.port_gerschgorin(rp, ci, v)
+    alpha, beta = 2.0 / (hi - lo), -(hi + lo) / (hi - lo)
+    if O.ref_available():
+        want = O.ref_basis(rp, ci, v, R, s, alpha, beta, cbcg=(m == 1))
+    else:
+        want = O.port_basis(rp, ci, v, R, s, alpha, beta)
+    d = {k: dev(torch, a) for k, a in dict(rp=rp, ci=ci, v=v, R=R).items()}
+    S = torch.zeros((n, s * m), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_basis(F64, n, ptr(d["rp"]), ptr(d["ci"]), ptr(d["v"]), ptr(d["R"]), m, s,
+                          alpha, beta, ptr(S), s * m, None)
+    assert rc == 0
+    assert relerr(host(S), want) <= 1e-12
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("n,ka,kb1,kb2", [(20000, 64, 64, 8), (50000, 96, 96, 16),
+                                          (3001, 12, 12, 3), (40000, 128, 128, 32),
+                                          (7, 4, 4, 1)])
+def test_gram_f64_matches_reference(lib, torch_cuda, variant, n, ka, kb1, kb2):
+    torch = torch_cuda
+    L = O.gen_rhs("normal", n, ka, 1)
+    R1 = O.gen_rhs("normal", n, kb1, 2)
+    R2 = O.gen_rhs("normal", n, kb2, 3)
+    want = O.port_gram(L, np.hstack([R1, R2]))
+    if O.ref_available() and n * ka <= 2_000_000:
+        assert np.array_equal(want, O.ref_gram(L, np.hstack([R1, R2])))
+    d = {k: dev(torch, a) for k, a in dict(L=L, R1=R1, R2=R2).items()}
+    C = torch.zeros((ka, kb1 + kb2), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_gram(F64, variant, n, ptr(d["L"]), ka, ka, ptr(d["R1"]), kb1, kb1,
+                         ptr(d["R2"]), kb2, kb2, ptr(C), kb1 + kb2, None)
+    assert rc == 0
+    assert relerr(host(C), want) <= 1e-12
+
+
+@pytest.mark.parametrize("n,ka,kb1,kb2", [(100000, 96, 96, 16), (5000, 24, 24, 4)])
+def test_gram_f32_fp64_accumulation(lib, torch_cuda, n, ka, kb1, kb2):
+    """FP32 inputs, FP64-accurate accumulation: matches the exact (FP64) Gram
+    of the FP32 values far below FP32 rounding."""
+    torch = torch_cuda
+    L = O.gen_rhs("normal", n, ka, 4).astype(np.float32)
+    R1 = O.gen_rhs("normal", n, kb1, 5).astype(np.float32)
+    R2 = O.gen_rhs("normal", n, kb2, 6).astype(np.float32)
+    want = O.port_gram(L.astype(np.float64), np.hstack([R1, R2]).astype(np.float64))
+    d = {k: dev(torch, a) for k, a in dict(L=L, R1=R1, R2=R2).items()}
+    C = torch.zeros((ka, kb1 + kb2), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_gram(F32, 0, n, ptr(d["L"]), ka, ka, ptr(d["R1"]), kb1, kb1, ptr(d["R2"]),
+                         kb2, kb2, ptr(C), kb1 + kb2, None)
+    assert rc == 0
+    assert relerr(host(C), want) <= 1e-10
+
+
+@pytest.mark.parametrize("vt", [F64, F32])
+@pytest.mark.parametrize("n,k", [(10000, 64), (30000, 96), (999, 12), (5000, 256)])
+def test_qupdate(lib, torch_cuda, vt, n, k):
+    torch = torch_cuda
+    Q = O.gen_rhs("normal", n, k, 1)
+    S = O.gen_rhs("normal", n, k, 2)
+    beta = O.gen_rhs("normal", k, k, 3)
+    dt = np.float64 if vt == F64 else np.float32
+    Qh, Sh = Q.astype(dt), S.astype(dt)
+    bh = beta if vt == F64 else beta.astype(np.float32).astype(np.float64)
+    want = Sh.astype(np.float64) - O.port_tallsmall(Qh.astype(np.float64), bh)
+    if vt == F64 and O.ref_available():
+        assert relerr(O.ref_tallsmall(Q, beta), O.port_tallsmall(Q, beta)) == 0.0
+    dq, ds, db = dev(torch, Qh), dev(torch, Sh), dev(torch, beta)
+    rc = lib.cacg_k_qupdate(vt, n, k, ptr(dq), k, ptr(ds), k, ptr(db), None)
+    assert rc == 0
+    assert relerr(host(dq), want) <= (1e-13 if vt == F64 else 3e-6)
+
+
+@pytest.mark.parametrize("vt", [F64, F32])
+@pytest.mark.parametrize("n,k,m", [(10000, 64, 8), (20000, 96, 16), (777, 4, 1),
+                                   (3000, 15, 5), (4000, 256, 32)])
+def test_xrupdate(lib, torch_cuda, vt, n, k, m):
+    torch = torch_cuda
+    dt = np.float64 if vt == F64 else np.float32
+    Q = O.gen_rhs("normal", n, k, 1).astype(dt)
+    AQ = O.gen_rhs("normal", n, k, 2).astype(dt)
+    al = O.gen_rhs("normal", k, m, 3)
+    X = O.gen_rhs("normal", n, m, 4)
+    R = O.gen_rhs("normal", n, m, 5)
+    Xw = X + O.port_tallsmall(Q.astype(np.float64), al)
+    Rw = R - O.port_tallsmall(AQ.astype(np.float64), al)
+    dQ, dAQ, dal, dX, dR = (dev(torch, a) for a in (Q, AQ, al, X, R))
+    S0 = torch.zeros((n, k), dtype=torch.float64 if vt == F64 else torch.float32, device="cuda")
+    norms = torch.zeros(m, dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_xrupdate(vt, n, k, m, ptr(dQ), ptr(dAQ), k, ptr(dal), ptr(dX), ptr(dR),
+                             ptr(S0), k, ptr(norms), None)
+    assert rc == 0
+    tol = 1e-13 if vt == F64 else 1e-11
+    assert relerr(host(dX), Xw) <= tol
+    assert relerr(host(dR), Rw) <= tol
+    Rg = host(dR)
+    assert relerr(host(S0)[:, :m], Rg) <= (0 if vt == F64 else 1e-7)
+    assert relerr(host(norms), (Rg * Rg).sum(axis=0)) <= 1e-13
+
+
+@pytest.mark.parametrize("k,r", [(4, 1), (64, 64), (64, 8), (96, 96), (96, 16), (128, 32),
+                                 (200, 20), (256, 32)])
+def test_lu_matches_reference(lib, torch_cuda, k, r):
+    torch = torch_cuda
+    G = O.gen_rhs("normal", 4 * k, k, 1)
+    M = G.T @ G / (4 * k) + np.eye(k)  # SPD, like Q^T A Q
+    RHS = O.gen_rhs("normal", k, r, 2)
+    want = O.ref_lu(M, RHS) if O.ref_available() else O.port_lu(M, RHS)
+    assert np.array_equal(want, O.port_lu(M, RHS))
+    dM, dR = dev(torch, M), dev(torch, RHS)
+    Y = torch.zeros((k, r), dtype=torch.float64, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rc = lib.cacg_k_lu(k, ptr(dM), r, ptr(dR), ptr(Y), ptr(st), None)
+    assert rc == 0
+    assert int(host(st)[0]) == 0
+    assert relerr(host(Y), want) <= 1e-11
+
+
+def test_lu_zero_pivot_sets_status(lib, torch_cuda):
+    torch = torch_cuda
+    k = 8
+    M = np.eye(k)
+    M[3, 3] = 0.0  # zero pivot: the reference divides by zero silently
+    dM, dR = dev(torch, M), dev(torch, np.ones((k, 2)))
+    Y = torch.zeros((k, 2), dtype=torch.float64, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rc = lib.cacg_k_lu(k, ptr(dM), 2, ptr(dR), ptr(Y), ptr(st), None)
+    assert rc == 0
+    assert int(host(st)[0]) & 1
+
+
+@pytest.mark.parametrize("kind,N", [("lap2d", 64), ("st3d27", 12), ("varcoef2d", 40)])
+def test_gerschgorin_exact(lib, torch_cuda, kind, N):
+    torch = torch_cuda
+    rp, ci, v = _mat(kind, N, shift=1e-6, sigma=1.5, seed=3)
+    want = O.ref_gerschgorin(rp, ci, v) if O.ref_available() else O.port_gerschgorin(rp, ci, v)
+    d = {k: dev(torch, a) for k, a in dict(rp=rp, ci=ci, v=v).items()}
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_gerschgorin(len(rp) - 1, ptr(d["rp"]), ptr(d["ci"]), ptr(d["v"]), ptr(out),
+                                None)
+    assert rc == 0
+    got = host(out)
+    # min/max of per-row sums: per-row sums are formed in the reference order
+    assert np.allclose(got, want, rtol=1e-14, atol=0)
