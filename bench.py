@@ -44,6 +44,17 @@ WORKLOADS = {
 CPU_SAMPLE_N = {"st27_128_m16": 48, "st27_32_m16": 16}
 
 
+def reduce_max(x: float, world: int, device=None) -> float:
+    """Max over ranks (the slowest replica sets the whole job's time)."""
+    if world <= 1:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def peaks():
     p = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -261,10 +272,7 @@ def run_gpu_arm(args, w, rank, world):
     clk = clocks.stop()
     lib.cacg_profile_enable(0)
     ms_total = e0.elapsed_time(e1)
-    t = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = reduce_max(ms_total, world, device="cuda")
     value = world * args.steps * m / (ms_max * 1e-3)
     relres = max(i["true_relres_max"] for i in infos)
     iters_mixed = infos[-1]["iterations"]
