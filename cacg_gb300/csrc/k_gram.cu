@@ -335,6 +335,7 @@ static GramPlan plan_gram(int variant, int64_t n, int ka, int kb) {
     if (nchunks < 1) nchunks = 1;
     p.rows_per_chunk = (n + nchunks - 1) / nchunks;
     p.rows_per_chunk = (p.rows_per_chunk + KT - 1) / KT * KT;
+    if (p.rows_per_chunk < KT) p.rows_per_chunk = KT;  // n == 0
     p.nchunks = (int)((n + p.rows_per_chunk - 1) / p.rows_per_chunk);
     if (p.nchunks < 1) p.nchunks = 1;
     if (variant == CACG_GRAM_DMMA) {
