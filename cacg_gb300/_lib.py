@@ -98,6 +98,10 @@ _SIGS = {
     "cacg_k_gram": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_int64,
                               C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p,
                               C.c_int64, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
+    "cacg_k_gram_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_int64,
+                                      C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p,
+                                      C.c_int64, C.c_int32, C.c_void_p, C.c_int32,
+                                      C.c_void_p]),
     "cacg_k_qupdate": (C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.c_void_p, C.c_int64,
                                  C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "cacg_k_xrupdate": (C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_void_p,

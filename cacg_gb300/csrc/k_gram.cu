@@ -454,3 +454,160 @@ extern "C" int cacg_k_gram(int32_t vtype, int32_t variant, int64_t n, const void
     cudaFreeAsync(ws, st);
     return rc;
 }
+
+// ---------------------------------------------------------------------------
+// Gram without device allocation.
+//
+// Some callers cannot let a library call cudaMalloc/cudaMallocAsync: processes
+// whose device memory is handed out by their own allocator (the whole pool
+// reserved up front, so a third-party allocation fails or breaks the budget),
+// and latency-critical loops where an allocation or free may synchronise the
+// device.  For them, cacg_k_gram_noalloc computes the same product as
+// cacg_k_gram, but its split-K partial tiles live in the fixed device array
+// below instead of a per-call workspace.
+//
+// * The array is 16 MiB, file-scope, and every GPU that loads libcacg.so holds
+//   it until the process exits.
+// * Shapes whose smallest split (one row chunk: tilesA*tilesB*BA*BB doubles)
+//   does not fit in it are rejected with CACG_ERR_ARG and a message; shapes
+//   that fit use as many row chunks as the array holds (fewer than
+//   cacg_k_gram may use, so the summation order, not the accuracy class,
+//   differs).
+// * All calls share the array and each call leaves its partial tiles in it.
+//   Every partial tile is fully overwritten by its CTA when n > 0; for n == 0
+//   the tiles are cleared with cudaMemsetAsync before the reduction.  Calls
+//   that overlap on the GPU (different streams, or different host threads)
+//   race on the array: serialise them.
+// * Device addresses: the host-side name of the array is not a device
+//   address.  The first call on each device (that device current) looks the
+//   address up once with cudaGetSymbolAddress and caches it; make that first
+//   call before any stream capture.
+// ---------------------------------------------------------------------------
+#include <cstdio>
+#include <mutex>
+
+namespace cacg {
+
+constexpr size_t kGramNoAllocScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) double
+    g_gram_noalloc_scratch[kGramNoAllocScratchBytes / sizeof(double)];
+
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[64];
+
+static int noalloc_scratch(double **out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return CACG_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        double *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_gram_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            record_cuda_error(e, "cudaGetSymbolAddress(g_gram_noalloc_scratch)", __FILE__,
+                              __LINE__);
+            cudaGetLastError();
+            return CACG_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return CACG_OK;
+}
+
+template <typename T>
+static int gram_fixed_scratch(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl,
+                              int ka, const T *R1, int64_t ldr1, int kb1, const T *R2,
+                              int64_t ldr2, int kb2, double *C1, int ldc1, double *C2, int ldc2,
+                              double *ws, size_t ws_bytes) {
+    const int kb = kb1 + kb2;
+    if (ka <= 0 || kb <= 0 || n < 0 || !C1 || (kb2 > 0 && !C2)) return CACG_ERR_ARG;
+    if (variant == CACG_GRAM_AUTO) variant = CACG_GRAM_FMA;
+    if (!std::is_same<T, double>::value) variant = CACG_GRAM_FMA;
+    if (variant == CACG_GRAM_DMMA) {
+        int BA = std::min(round_up(ka, 8), kMaxTile), BB = std::min(round_up(kb, 8), kMaxTile);
+        if ((BA / 8) * (BB / 8) > 16 * kDmmaMaxTilesPerWarp) variant = CACG_GRAM_FMA;
+    }
+    GramPlan p = plan_gram<T>(variant, n, ka, kb);
+    const size_t per_chunk = (size_t)p.tilesA * p.tilesB * p.BA * p.BB * sizeof(double);
+    if (per_chunk > ws_bytes) {
+        fprintf(stderr,
+                "cacg_k_gram_noalloc: a %d x %d Gram needs %zu bytes of scratch per row chunk; "
+                "the fixed scratch holds %zu bytes\n",
+                ka, kb, per_chunk, ws_bytes);
+        return CACG_ERR_ARG;
+    }
+    const int64_t max_chunks = (int64_t)(ws_bytes / per_chunk);
+    if (p.nchunks > max_chunks) {
+        const int KT = (variant == CACG_GRAM_DMMA) ? 16 : GramKT<T>::value;
+        p.rows_per_chunk = (n + max_chunks - 1) / max_chunks;
+        p.rows_per_chunk = (p.rows_per_chunk + KT - 1) / KT * KT;
+        p.nchunks = (int)((n + p.rows_per_chunk - 1) / p.rows_per_chunk);
+        if (p.nchunks < 1) p.nchunks = 1;
+    }
+    const size_t need = (size_t)p.nchunks * per_chunk;
+    dim3 grid(p.nchunks, p.tilesA * p.tilesB);
+    if (n > 0) {
+        if (variant == CACG_GRAM_DMMA) {
+            if constexpr (std::is_same<T, double>::value) {
+                static const bool attr = [] {
+                    cudaFuncSetAttribute(gram_dmma_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)max_smem_optin());
+                    return true;
+                }();
+                (void)attr;
+                gram_dmma_kernel<<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl,
+                                                                  ka, R1, ldr1, kb1, R2, ldr2,
+                                                                  kb2, p.BA, p.BB, p.tilesB,
+                                                                  ws);
+            }
+        } else {
+            static const bool attr = [] {
+                cudaFuncSetAttribute(gram_fma_kernel<T>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)max_smem_optin());
+                return true;
+            }();
+            (void)attr;
+            gram_fma_kernel<T><<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl,
+                                                                ka, R1, ldr1, kb1, R2, ldr2,
+                                                                kb2, p.BA, p.BB, p.tilesB, ws);
+        }
+        int rc = check_launch();
+        if (rc != CACG_OK) return rc;
+    } else {
+        if (cudaMemsetAsync(ws, 0, need, st) != cudaSuccess) return CACG_ERR_CUDA;
+    }
+    int tot = ka * kb;
+    gram_reduce_kernel<<<(tot + 255) / 256, 256, 0, st>>>(ws, n > 0 ? p.nchunks : 1,
+                                                          p.tilesA * p.tilesB, p.BA, p.BB,
+                                                          p.tilesB, ka, kb, kb1, C1, ldc1,
+                                                          C2, ldc2);
+    return check_launch();
+}
+
+}  // namespace cacg
+
+extern "C" int cacg_k_gram_noalloc(int32_t vtype, int32_t variant, int64_t n, const void *L,
+                                   int64_t ldl, int32_t ka, const void *R1, int64_t ldr1,
+                                   int32_t kb1, const void *R2, int64_t ldr2, int32_t kb2,
+                                   double *C, int32_t ldc, void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (kb2 > 0 && !R2) return CACG_ERR_ARG;
+    double *ws = nullptr;
+    int rc = noalloc_scratch(&ws);
+    if (rc != CACG_OK) return rc;
+    const size_t wsb = kGramNoAllocScratchBytes;
+    if (vtype == CACG_VAL_F64)
+        return gram_fixed_scratch<double>(st, variant, n, (const double *)L, ldl, ka,
+                                          (const double *)R1, ldr1, kb1, (const double *)R2,
+                                          ldr2, kb2, C, ldc, C + kb1, ldc, ws, wsb);
+    if (vtype == CACG_VAL_F32)
+        return gram_fixed_scratch<float>(st, variant, n, (const float *)L, ldl, ka,
+                                         (const float *)R1, ldr1, kb1, (const float *)R2, ldr2,
+                                         kb2, C, ldc, C + kb1, ldc, ws, wsb);
+    return CACG_ERR_ARG;
+}

@@ -192,6 +192,20 @@ int cacg_k_gram(int32_t vtype, int32_t variant, int64_t n, const void *L, int64_
                 int32_t ka, const void *R1, int64_t ldr1, int32_t kb1, const void *R2,
                 int64_t ldr2, int32_t kb2, double *C, int32_t ldc, void *stream);
 
+/* No counterpart in the reference.  Same product as cacg_k_gram, for callers
+ * that cannot let the library allocate device memory (their device memory is
+ * owned by their own allocator, or an allocation could synchronise a
+ * latency-critical loop): the split-K scratch is a fixed 16 MiB device array
+ * inside libcacg.so, held by every GPU that loads the library until exit.
+ * Calls no cudaMalloc/cudaFree.  Shapes whose single-chunk scratch exceeds
+ * 16 MiB return CACG_ERR_ARG.  All calls share the array: calls that overlap
+ * on the GPU race.  The first call on a device looks up the array's device
+ * address; make it before any stream capture. */
+int cacg_k_gram_noalloc(int32_t vtype, int32_t variant, int64_t n, const void *L,
+                        int64_t ldl, int32_t ka, const void *R1, int64_t ldr1, int32_t kb1,
+                        const void *R2, int64_t ldr2, int32_t kb2, double *C, int32_t ldc,
+                        void *stream);
+
 /* src/BLAS3.c:794-825 + :579-612 fused: Q = S - Q * beta (in place on Q),
  * Q, S n x k (strides ldq, lds), beta k x k FP64 row-major. */
 int cacg_k_qupdate(int32_t vtype, int64_t n, int32_t k, void *Q, int64_t ldq,
