@@ -18,7 +18,7 @@ ERR_UNSUPPORTED, ERR_BUSY, ERR_NODEV = -6, -7, -8
 BOUNDS_GERSCHGORIN, BOUNDS_GIVEN, BOUNDS_LANCZOS = 0, 1, 2
 TOL_ABS_COL0, TOL_REL_ALL = 0, 1
 FP64, MIXED = 0, 1
-GRAM_AUTO, GRAM_FMA, GRAM_DMMA = 0, 1, 2
+GRAM_AUTO, GRAM_FMA, GRAM_DMMA, GRAM_TC = 0, 1, 2, 3
 VAL_F64, VAL_F32 = 0, 1
 
 
@@ -34,7 +34,7 @@ class CacgParams(C.Structure):
                 ("precision", C.c_int32), ("rr_period", C.c_int32),
                 ("gram_variant", C.c_int32), ("lanczos_seed", C.c_uint64),
                 ("stream", C.c_void_p), ("use_graph", C.c_int32),
-                ("reserved", C.c_int32 * 7)]
+                ("exact_updates", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class CacgResult(C.Structure):

@@ -96,6 +96,13 @@ int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl
                 double *C1, int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes);
 size_t gram_workspace_bytes(int64_t n, int ka, int kb);
 
+// Tensor-core Gram of FP32 blocks (three bf16 slices per value, six slice
+// products, FP32 accumulation over 256-row groups, FP64 across groups).
+int launch_gram_tc(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int ka,
+                   const float *R1, int64_t ldr1, int kb1, const float *R2, int64_t ldr2, int kb2,
+                   double *C1, int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes);
+size_t gram_tc_workspace_bytes(int64_t n, int ka, int kb);
+
 // Q_out = S - Q_in * beta  (Q_out may alias S; never Q_in).
 template <typename T>
 int launch_qupdate(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo,
@@ -107,6 +114,11 @@ int launch_xrupdate(cudaStream_t st, int64_t n, int k, int m, const T *Q, const 
                     int64_t ldq, const double *alpha, double *X, double *R, T *S0,
                     int64_t lds, float *R32, double *norms, double *ws);
 size_t norm_workspace_doubles(int64_t n, int m);
+// Same update with the k-term products accumulated in T (FP32 FMAs for float).
+template <typename T>
+int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,
+                         int64_t ldq, const double *alpha, double *X, double *R, T *S0,
+                         int64_t lds, float *R32, double *norms, double *ws);
 
 // Small LU (Crout, U unit diagonal, no pivoting).
 int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *status);

@@ -420,6 +420,15 @@ int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl
     return check_launch();
 }
 
+int launch_gram_reduce(cudaStream_t st, const double *part, int nchunks, int ntiles, int BA,
+                       int BB, int tilesB, int ka, int kb, int kb1, double *C1, int ldc1,
+                       double *C2, int ldc2) {
+    int tot = ka * kb;
+    gram_reduce_kernel<<<(tot + 255) / 256, 256, 0, st>>>(part, nchunks, ntiles, BA, BB, tilesB,
+                                                          ka, kb, kb1, C1, ldc1, C2, ldc2);
+    return check_launch();
+}
+
 template int launch_gram<double>(cudaStream_t, int, int64_t, const double *, int64_t, int,
                                  const double *, int64_t, int, const double *, int64_t, int,
                                  double *, int, double *, int, double *, size_t);
@@ -437,6 +446,16 @@ extern "C" int cacg_k_gram(int32_t vtype, int32_t variant, int64_t n, const void
                            void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (kb2 > 0 && !R2) return CACG_ERR_ARG;
+    if (variant == CACG_GRAM_TC) {
+        if (vtype != CACG_VAL_F32) return CACG_ERR_ARG;
+        size_t wsb = gram_tc_workspace_bytes(n, ka, kb1 + kb2);
+        double *w = nullptr;
+        if (cudaMallocAsync((void **)&w, wsb > 0 ? wsb : 16, st) != cudaSuccess) return CACG_ERR_OOM;
+        int rc = launch_gram_tc(st, n, (const float *)L, ldl, ka, (const float *)R1, ldr1, kb1,
+                                (const float *)R2, ldr2, kb2, C, ldc, C + kb1, ldc, w, wsb);
+        cudaFreeAsync(w, st);
+        return rc;
+    }
     size_t ws_bytes = gram_workspace_bytes(n, ka, kb1 + kb2);
     double *ws = nullptr;
     if (cudaMallocAsync((void **)&ws, ws_bytes, st) != cudaSuccess) return CACG_ERR_OOM;

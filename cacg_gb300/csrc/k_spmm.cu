@@ -26,6 +26,7 @@ namespace cacg {
 
 constexpr int kSpmmThreads = 256;
 constexpr int kMaxNch = 4;
+constexpr int kGroup = 8;  // nonzeros fetched together per lane
 
 template <typename T, int CH>
 __device__ __forceinline__ void load_chunk(T (&d)[CH], const T *p) {
@@ -56,32 +57,57 @@ __device__ __forceinline__ void store_chunk(T *p, const T (&d)[CH]) {
 
 // One team of TEAM lanes per row; lane lt owns chunks lt, lt+TEAM, ... (nch of them)
 // of this column block (blockIdx.y).
-template <typename T, int CH, int TEAM>
+template <typename T, int CH, int TEAM, int NCH>
 __global__ void __launch_bounds__(kSpmmThreads)
     spmm_rows_kernel(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
-                     const T *__restrict__ val, int w, int nch, const T *__restrict__ X,
+                     const T *__restrict__ val, int w, const T *__restrict__ X,
                      int64_t ldx, T *__restrict__ Y, int64_t ldy, const T *__restrict__ Z1,
                      int64_t ldz1, const T *__restrict__ Z2, int64_t ldz2, T ca, T cb, T cc) {
     const int lt = threadIdx.x % TEAM;
     const int64_t team0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TEAM;
     const int64_t nteams = ((int64_t)gridDim.x * blockDim.x) / TEAM;
-    const int colbase = blockIdx.y * (TEAM * kMaxNch * CH);
+    const int colbase = blockIdx.y * (TEAM * NCH * CH);
     for (int64_t row = team0; row < n; row += nteams) {
-        T acc[kMaxNch][CH];
+        T acc[NCH][CH];
 #pragma unroll
-        for (int j = 0; j < kMaxNch; ++j)
+        for (int j = 0; j < NCH; ++j)
 #pragma unroll
             for (int q = 0; q < CH; ++q) acc[j][q] = T(0);
         const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
-#pragma unroll 2
-        for (int p = b; p < e; ++p) {
+        int p = b;
+        // groups of kGroup nonzeros: all index/value loads first, then all
+        // gathers, so each lane keeps kGroup independent loads in flight
+        for (; p + kGroup <= e; p += kGroup) {
+            int cg[kGroup];
+            T ag[kGroup];
+#pragma unroll
+            for (int u = 0; u < kGroup; ++u) {
+                cg[u] = __ldg(ci + p + u);
+                ag[u] = __ldg(val + p + u);
+            }
+#pragma unroll
+            for (int j = 0; j < NCH; ++j) {
+                const int col = (lt + j * TEAM) * CH;
+                if (colbase + col < w) {
+                    T x[kGroup][CH];
+#pragma unroll
+                    for (int u = 0; u < kGroup; ++u)
+                        load_chunk<T, CH>(x[u], X + (int64_t)cg[u] * ldx + colbase + col);
+#pragma unroll
+                    for (int u = 0; u < kGroup; ++u)
+#pragma unroll
+                        for (int q = 0; q < CH; ++q) acc[j][q] = fma(ag[u], x[u][q], acc[j][q]);
+                }
+            }
+        }
+        for (; p < e; ++p) {
             const int c = __ldg(ci + p);
             const T a = __ldg(val + p);
             const T *xr = X + (int64_t)c * ldx + colbase;
 #pragma unroll
-            for (int j = 0; j < kMaxNch; ++j) {
+            for (int j = 0; j < NCH; ++j) {
                 const int col = (lt + j * TEAM) * CH;
-                if (j < nch && colbase + col < w) {
+                if (colbase + col < w) {
                     T x[CH];
                     load_chunk<T, CH>(x, xr + col);
 #pragma unroll
@@ -90,9 +116,9 @@ __global__ void __launch_bounds__(kSpmmThreads)
             }
         }
 #pragma unroll
-        for (int j = 0; j < kMaxNch; ++j) {
+        for (int j = 0; j < NCH; ++j) {
             const int col = colbase + (lt + j * TEAM) * CH;
-            if (j < nch && col < w) {
+            if (col < w) {
                 T y[CH];
 #pragma unroll
                 for (int q = 0; q < CH; ++q) y[q] = ca * acc[j][q];
@@ -131,6 +157,7 @@ __global__ void __launch_bounds__(kSpmmThreads)
         T acc = T(0);
         if (row < n) {
             const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
+#pragma unroll 4
             for (int p = b + lt; p < e; p += TEAM)
                 acc = fma(__ldg(val + p), __ldg(X + (int64_t)__ldg(ci + p) * ldx), acc);
         }
@@ -155,27 +182,27 @@ static int grid_for(int64_t units, int threads_per_unit_den) {
     return (int)blocks;
 }
 
-template <typename T, int CH, int TEAM>
+template <typename T, int CH, int TEAM, int NCH>
 static int launch_rows(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
-                       const T *val, int w, int nch, int ycols, const T *X, int64_t ldx, T *Y,
+                       const T *val, int w, int ycols, const T *X, int64_t ldx, T *Y,
                        int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2, int64_t ldz2, T ca,
                        T cb, T cc) {
     const int rows_per_block = kSpmmThreads / TEAM;
     dim3 grid(grid_for(n, rows_per_block), ycols);
-    spmm_rows_kernel<T, CH, TEAM><<<grid, kSpmmThreads, 0, st>>>(
-        n, rp, ci, val, w, nch, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc);
+    spmm_rows_kernel<T, CH, TEAM, NCH><<<grid, kSpmmThreads, 0, st>>>(
+        n, rp, ci, val, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc);
     return check_launch();
 }
 
-template <typename T, int CH>
+template <typename T, int CH, int NCH>
 static int dispatch_team(int team, cudaStream_t st, int64_t n, const int32_t *rp,
-                         const int32_t *ci, const T *val, int w, int nch, int ycols,
-                         const T *X, int64_t ldx, T *Y, int64_t ldy, const T *Z1,
-                         int64_t ldz1, const T *Z2, int64_t ldz2, T ca, T cb, T cc) {
-#define CACG_TEAM_CASE(TM)                                                              \
-    case TM:                                                                            \
-        return launch_rows<T, CH, TM>(st, n, rp, ci, val, w, nch, ycols, X, ldx, Y, ldy, \
-                                      Z1, ldz1, Z2, ldz2, ca, cb, cc);
+                         const int32_t *ci, const T *val, int w, int ycols, const T *X,
+                         int64_t ldx, T *Y, int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2,
+                         int64_t ldz2, T ca, T cb, T cc) {
+#define CACG_TEAM_CASE(TM)                                                                \
+    case TM:                                                                              \
+        return launch_rows<T, CH, TM, NCH>(st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1, \
+                                           ldz1, Z2, ldz2, ca, cb, cc);
     switch (team) {
         CACG_TEAM_CASE(1)
         CACG_TEAM_CASE(2)
@@ -186,6 +213,27 @@ static int dispatch_team(int team, cudaStream_t st, int64_t n, const int32_t *rp
     }
 #undef CACG_TEAM_CASE
     return CACG_ERR_ARG;
+}
+
+template <typename T, int CH>
+static int dispatch_nch(int nch, int team, cudaStream_t st, int64_t n, const int32_t *rp,
+                        const int32_t *ci, const T *val, int w, int ycols, const T *X,
+                        int64_t ldx, T *Y, int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2,
+                        int64_t ldz2, T ca, T cb, T cc) {
+    switch (nch) {
+    case 1:
+        return dispatch_team<T, CH, 1>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
+                                       ldz1, Z2, ldz2, ca, cb, cc);
+    case 2:
+        return dispatch_team<T, CH, 2>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
+                                       ldz1, Z2, ldz2, ca, cb, cc);
+    case 3:
+        return dispatch_team<T, CH, 3>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
+                                       ldz1, Z2, ldz2, ca, cb, cc);
+    default:
+        return dispatch_team<T, CH, 4>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
+                                       ldz1, Z2, ldz2, ca, cb, cc);
+    }
 }
 
 template <typename T>
@@ -239,10 +287,10 @@ int launch_spmm(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci
     int nch = ycols > 1 ? kMaxNch : best_nch;
     int yc = ycols > 1 ? (chunks + best_team * kMaxNch - 1) / (best_team * kMaxNch) : 1;
     if (vec)
-        return dispatch_team<T, VN>(best_team, st, n, rp, ci, val, w, nch, yc, X, ldx, Y, ldy,
-                                    Z1, ldz1, Z2, ldz2, ca, cb, cc);
-    return dispatch_team<T, 1>(best_team, st, n, rp, ci, val, w, nch, yc, X, ldx, Y, ldy, Z1,
-                               ldz1, Z2, ldz2, ca, cb, cc);
+        return dispatch_nch<T, VN>(nch, best_team, st, n, rp, ci, val, w, yc, X, ldx, Y, ldy, Z1,
+                                   ldz1, Z2, ldz2, ca, cb, cc);
+    return dispatch_nch<T, 1>(nch, best_team, st, n, rp, ci, val, w, yc, X, ldx, Y, ldy, Z1,
+                              ldz1, Z2, ldz2, ca, cb, cc);
 }
 
 template int launch_spmm<double>(cudaStream_t, int64_t, const int32_t *, const int32_t *,

@@ -14,6 +14,7 @@
 //
 // Reductions (norms, bounds, dots) are two-pass with a fixed grid and fixed
 // order, hence deterministic.
+#include <algorithm>
 #include <cfloat>
 
 #include "cacg_internal.cuh"
@@ -23,11 +24,19 @@ namespace cacg {
 constexpr int kRowThreads = 256;
 constexpr int kRedBlocks = 304;  // fixed partial count for two-pass reductions
 
+template <typename T>
+static bool direct_ok(int k, int64_t ld, const void *a, const void *b);
+template <typename T>
+int launch_xrupdate_direct(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,
+                           int64_t ldq, const double *alpha, double *X, double *R, T *S0,
+                           int64_t lds, float *R32, double *norms, double *ws);
+
 // --------------------------------------------------------------- qupdate
-// Qout[i][c] = S[i][c] - sum_j Qin[i][j] * W[j][c] ; W = beta (k x k FP64),
-// staged in shared memory as T, in column blocks of BC.
-constexpr int kQuTR = 32;  // rows per tile
-constexpr int kQuM = 4;    // micro tile rows
+// Qout[i][c] = S[i][c] - sum_j Qin[i][j] * W[j][c]; W = beta (k x k FP64)
+// staged in shared memory as T in column blocks of BC; the Qin tile is staged
+// transposed (Qt[j][r]) so a thread's 8 rows are two 16-byte vectors.
+constexpr int kQuTR = 64;  // rows per tile
+constexpr int kQuM = 8;    // micro tile rows
 constexpr int kQuN = 4;    // micro tile cols
 
 template <typename T>
@@ -36,8 +45,9 @@ __global__ void __launch_bounds__(512)
                    int64_t ldq, const T *S, int64_t lds, const double *__restrict__ beta) {
     // Qout may alias S (each element is read, then written, by one thread)
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *Ws = reinterpret_cast<T *>(smem_raw);  // k x BC
-    T *Qs = Ws + (size_t)k * BC;              // kQuTR x k
+    constexpr int TRP = kQuTR + 16 / sizeof(T);  // padded row length of Qt
+    T *Ws = reinterpret_cast<T *>(smem_raw);      // k x BC
+    T *Qt = Ws + (size_t)k * BC;                  // k x TRP
     const int c0 = blockIdx.y * BC;
     const int bc = min(BC, k - c0);
     for (int idx = threadIdx.x; idx < k * BC; idx += blockDim.x) {
@@ -52,7 +62,7 @@ __global__ void __launch_bounds__(512)
         for (int idx = threadIdx.x; idx < kQuTR * k; idx += blockDim.x) {
             int r = idx / k, j = idx % k;
             int64_t row = r0 + r;
-            Qs[idx] = row < n ? Qin[row * ldq + j] : T(0);
+            Qt[j * TRP + r] = row < n ? Qin[row * ldq + j] : T(0);
         }
         __syncthreads();
         if (active) {
@@ -61,10 +71,11 @@ __global__ void __launch_bounds__(512)
             for (int i = 0; i < kQuM; ++i)
 #pragma unroll
                 for (int q = 0; q < kQuN; ++q) acc[i][q] = T(0);
+#pragma unroll 2
             for (int j = 0; j < k; ++j) {
                 T qv[kQuM], wv[kQuN];
 #pragma unroll
-                for (int i = 0; i < kQuM; ++i) qv[i] = Qs[(tr * kQuM + i) * k + j];
+                for (int i = 0; i < kQuM; ++i) qv[i] = Qt[j * TRP + tr * kQuM + i];
 #pragma unroll
                 for (int q = 0; q < kQuN; ++q) wv[q] = Ws[j * BC + tc * kQuN + q];
 #pragma unroll
@@ -87,20 +98,28 @@ __global__ void __launch_bounds__(512)
 }
 
 template <typename T>
+int launch_qupdate_direct(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo,
+                          const T *Qin, int64_t ldq, const T *S, int64_t lds,
+                          const double *beta);
+
+template <typename T>
 int launch_qupdate(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo, const T *Qin,
                    int64_t ldq, const T *S, int64_t lds, const double *beta) {
     if (n <= 0) return CACG_OK;
     if (k <= 0 || (const void *)Qout == (const void *)Qin) return CACG_ERR_ARG;
-    // column block: whole k when W and the Q tile fit comfortably
+    if (k % 4 == 0 && k / 4 <= 256 && ldq % 4 == 0 && (size_t)k * k * sizeof(T) <= 160 * 1024 &&
+        aligned16(Qin))
+        return launch_qupdate_direct<T>(st, n, k, Qout, ldo, Qin, ldq, S, lds, beta);
+    constexpr int TRP = kQuTR + 16 / sizeof(T);
     size_t budget = max_smem_optin() - 1024;
+    auto need = [&](int bc) { return ((size_t)k * bc + (size_t)k * TRP) * sizeof(T); };
     int BC = (k + kQuN - 1) / kQuN * kQuN;
-    while (BC > kQuN && ((size_t)k * BC + (size_t)kQuTR * k) * sizeof(T) > budget)
-        BC = (BC / 2 + kQuN - 1) / kQuN * kQuN;
-    if (((size_t)k * BC + (size_t)kQuTR * k) * sizeof(T) > budget) return CACG_ERR_UNSUPPORTED;
+    while (BC > kQuN && need(BC) > budget) BC = (BC / 2 + kQuN - 1) / kQuN * kQuN;
+    while (BC > kQuN && (kQuTR / kQuM) * (BC / kQuN) > 512) BC -= kQuN;
+    if (need(BC) > budget) return CACG_ERR_UNSUPPORTED;
     int threads = (kQuTR / kQuM) * (BC / kQuN);
     threads = (threads + 31) / 32 * 32;
-    if (threads > 512) return CACG_ERR_UNSUPPORTED;
-    size_t smem = ((size_t)k * BC + (size_t)kQuTR * k) * sizeof(T);
+    size_t smem = need(BC);
     static const bool attr = [] {
         cudaFuncSetAttribute(qupdate_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)max_smem_optin());
@@ -229,7 +248,7 @@ __global__ void colsum_kernel(const double *__restrict__ part, int G, int m,
 
 size_t norm_workspace_doubles(int64_t n, int m) {
     (void)n;
-    return (size_t)kRedBlocks * (size_t)(m > 0 ? m : 1);
+    return (size_t)2048 * (size_t)(m > 0 ? m : 1);  // >= kRedBlocks and kXrMaxBlocks
 }
 
 static int pow2ceil(int x) {
@@ -272,6 +291,349 @@ template int launch_xrupdate<double>(cudaStream_t, int64_t, int, int, const doub
 template int launch_xrupdate<float>(cudaStream_t, int64_t, int, int, const float *,
                                     const float *, int64_t, const double *, double *, double *,
                                     float *, int64_t, float *, double *, double *);
+
+// ------------------------------------------------- xrupdate (fast path)
+// X += Q alpha; R -= AQ alpha with products accumulated in T (FP32 FMAs in the
+// mixed mode, FP64 in the FP64 mode); the X/R additions are FP64.  A thread
+// owns one row and 4 consecutive columns; Q and AQ tiles are staged in shared
+// memory with a padded row length, alpha as T.
+constexpr int kXrG = 4;  // columns per thread
+
+template <typename T>
+__global__ void __launch_bounds__(kRowThreads)
+    xrupdate_fast_kernel(int64_t n, int k, int m, const T *__restrict__ Q,
+                         const T *__restrict__ AQ, int64_t ldq, const double *__restrict__ alpha,
+                         double *__restrict__ X, double *__restrict__ R, T *__restrict__ S0,
+                         int64_t lds, float *__restrict__ R32, double *__restrict__ part) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int G = (m + kXrG - 1) / kXrG;  // column groups per row
+    const int mp = G * kXrG;
+    const int TR = blockDim.x / G;        // rows per tile
+    const int kp = k + 16 / (int)sizeof(T);
+    T *As = reinterpret_cast<T *>(smem_raw);  // k x mp
+    T *Qs = As + (size_t)k * mp;              // TR x kp
+    T *AQs = Qs + (size_t)TR * kp;            // TR x kp
+    double *red = reinterpret_cast<double *>(AQs + (size_t)TR * kp);  // TR x mp
+    for (int idx = threadIdx.x; idx < k * mp; idx += blockDim.x) {
+        int j = idx / mp, c = idx % mp;
+        As[idx] = c < m ? T(alpha[(size_t)j * m + c]) : T(0);
+    }
+    const int r = threadIdx.x / G, g = threadIdx.x % G;
+    const bool active = r < TR;
+    double sq[kXrG] = {0.0, 0.0, 0.0, 0.0};
+    for (int64_t r0 = (int64_t)blockIdx.x * TR; r0 < n; r0 += (int64_t)gridDim.x * TR) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < TR * k; idx += blockDim.x) {
+            int rr = idx / k, j = idx % k;
+            int64_t row = r0 + rr;
+            Qs[rr * kp + j] = row < n ? Q[row * ldq + j] : T(0);
+            AQs[rr * kp + j] = row < n ? AQ[row * ldq + j] : T(0);
+        }
+        __syncthreads();
+        const int64_t row = r0 + r;
+        if (active && row < n) {
+            T ax[kXrG], ar[kXrG];
+#pragma unroll
+            for (int q = 0; q < kXrG; ++q) ax[q] = ar[q] = T(0);
+#pragma unroll 4
+            for (int j = 0; j < k; ++j) {
+                const T qv = Qs[r * kp + j], aqv = AQs[r * kp + j];
+                const T *aj = As + (size_t)j * mp + g * kXrG;
+#pragma unroll
+                for (int q = 0; q < kXrG; ++q) {
+                    ax[q] = fma(qv, aj[q], ax[q]);
+                    ar[q] = fma(aqv, aj[q], ar[q]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kXrG; ++q) {
+                const int c = g * kXrG + q;
+                if (c < m) {
+                    double x = X[row * m + c] + (double)ax[q];
+                    double rv = R[row * m + c] - (double)ar[q];
+                    X[row * m + c] = x;
+                    R[row * m + c] = rv;
+                    if (S0) S0[row * lds + c] = (T)rv;
+                    if (R32) R32[row * m + c] = (float)rv;
+                    sq[q] = fma(rv, rv, sq[q]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (part) {
+        if (active)
+#pragma unroll
+            for (int q = 0; q < kXrG; ++q) red[r * mp + g * kXrG + q] = sq[q];
+        __syncthreads();
+        for (int c = threadIdx.x; c < m; c += blockDim.x) {
+            double s = 0.0;
+            for (int rr = 0; rr < TR; ++rr) s += red[rr * mp + c];
+            part[(size_t)blockIdx.x * m + c] = s;
+        }
+    }
+}
+
+template <typename T>
+int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,
+                         int64_t ldq, const double *alpha, double *X, double *R, T *S0,
+                         int64_t lds, float *R32, double *norms, double *ws) {
+    if (m <= 0 || k <= 0) return CACG_ERR_ARG;
+    if (norms && !ws) return CACG_ERR_ARG;
+    if (direct_ok<T>(k, ldq, Q, AQ))
+        return launch_xrupdate_direct<T>(st, n, k, m, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms,
+                                         ws);
+    const int G = (m + kXrG - 1) / kXrG;
+    if (G > kRowThreads) return CACG_ERR_ARG;
+    const int mp = G * kXrG;
+    const int TR = kRowThreads / G;
+    const int kp = k + 16 / (int)sizeof(T);
+    size_t smem = ((size_t)k * mp + 2 * (size_t)TR * kp) * sizeof(T) + (size_t)TR * mp * 8 + 16;
+    if (smem > max_smem_optin()) return CACG_ERR_UNSUPPORTED;
+    static const bool attr = [] {
+        cudaFuncSetAttribute(xrupdate_fast_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    int G2 = kRedBlocks;
+    int64_t tiles = (n + TR - 1) / TR;
+    if (tiles < G2) G2 = (int)(tiles > 0 ? tiles : 1);
+    xrupdate_fast_kernel<T><<<G2, kRowThreads, smem, st>>>(n, k, m, Q, AQ, ldq, alpha, X, R, S0,
+                                                           lds, R32, norms ? ws : nullptr);
+    int rc = check_launch();
+    if (rc != CACG_OK || !norms) return rc;
+    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G2, m, norms);
+    return check_launch();
+}
+
+template int launch_xrupdate_fast<double>(cudaStream_t, int64_t, int, int, const double *,
+                                          const double *, int64_t, const double *, double *,
+                                          double *, double *, int64_t, float *, double *,
+                                          double *);
+template int launch_xrupdate_fast<float>(cudaStream_t, int64_t, int, int, const float *,
+                                         const float *, int64_t, const double *, double *,
+                                         double *, float *, int64_t, float *, double *, double *);
+
+// ----------------------------------------------- direct-load update kernels
+// Tall operand rows are read straight from global memory as 16-byte vectors
+// (threads sharing a row hit the same L1 lines), the small coefficient matrix
+// lives in shared memory as T, and there is no per-tile staging or barrier.
+// Used when k and the row strides are multiples of the vector width.
+
+// Qout[i][c..c+3] = S[i][c..c+3] - sum_j Qin[i][j] beta[j][c..c+3]; a thread
+// owns kDqRows rows x 4 columns.
+constexpr int kDqRows = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    qupdate_direct_kernel(int64_t n, int k, T *Qout, int64_t ldo, const T *__restrict__ Qin,
+                          int64_t ldq, const T *S, int64_t lds, const double *__restrict__ beta) {
+    // Qout may alias S (each element is read, then written, by one thread)
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *Ws = reinterpret_cast<T *>(smem_raw);  // k x k
+    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) Ws[idx] = T(beta[idx]);
+    __syncthreads();
+    const int G = k / 4;                       // column groups
+    const int groups_per_block = blockDim.x / G;
+    const int lg = threadIdx.x / G, cg = threadIdx.x % G;
+    if (lg >= groups_per_block) return;
+    const int64_t ngroups = (n + kDqRows - 1) / kDqRows;
+    for (int64_t rg = (int64_t)blockIdx.x * groups_per_block + lg; rg < ngroups;
+         rg += (int64_t)gridDim.x * groups_per_block) {
+        const int64_t r0 = rg * kDqRows;
+        T acc[kDqRows][4];
+#pragma unroll
+        for (int i = 0; i < kDqRows; ++i)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[i][q] = T(0);
+        for (int j = 0; j < k; j += 4) {
+            T qv[kDqRows][4];
+#pragma unroll
+            for (int i = 0; i < kDqRows; ++i) {
+                const int64_t row = r0 + i < n ? r0 + i : n - 1;
+                if constexpr (sizeof(T) == 4) {
+                    float4 v = __ldg(reinterpret_cast<const float4 *>(Qin + row * ldq + j));
+                    qv[i][0] = v.x; qv[i][1] = v.y; qv[i][2] = v.z; qv[i][3] = v.w;
+                } else {
+                    double2 v0 = __ldg(reinterpret_cast<const double2 *>(Qin + row * ldq + j));
+                    double2 v1 = __ldg(reinterpret_cast<const double2 *>(Qin + row * ldq + j + 2));
+                    qv[i][0] = v0.x; qv[i][1] = v0.y; qv[i][2] = v1.x; qv[i][3] = v1.y;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const T *w = Ws + (size_t)(j + u) * k + cg * 4;
+                T w0, w1, w2, w3;
+                if constexpr (sizeof(T) == 4) {
+                    float4 wv = *reinterpret_cast<const float4 *>(w);
+                    w0 = wv.x; w1 = wv.y; w2 = wv.z; w3 = wv.w;
+                } else {
+                    double2 wa = *reinterpret_cast<const double2 *>(w);
+                    double2 wb = *reinterpret_cast<const double2 *>(w + 2);
+                    w0 = wa.x; w1 = wa.y; w2 = wb.x; w3 = wb.y;
+                }
+#pragma unroll
+                for (int i = 0; i < kDqRows; ++i) {
+                    acc[i][0] = fma(qv[i][u], w0, acc[i][0]);
+                    acc[i][1] = fma(qv[i][u], w1, acc[i][1]);
+                    acc[i][2] = fma(qv[i][u], w2, acc[i][2]);
+                    acc[i][3] = fma(qv[i][u], w3, acc[i][3]);
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < kDqRows; ++i) {
+            const int64_t row = r0 + i;
+            if (row >= n) break;
+            const T *sp = S + row * lds + cg * 4;
+            T *op = Qout + row * ldo + cg * 4;
+            T s0 = sp[0], s1 = sp[1], s2 = sp[2], s3 = sp[3];
+            op[0] = s0 - acc[i][0];
+            op[1] = s1 - acc[i][1];
+            op[2] = s2 - acc[i][2];
+            op[3] = s3 - acc[i][3];
+        }
+    }
+}
+
+// X += Q alpha; R -= AQ alpha (products in T, additions in FP64); a thread
+// owns one row x 4 columns; norms partials per block.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    xrupdate_direct_kernel(int64_t n, int k, int m, const T *__restrict__ Q,
+                           const T *__restrict__ AQ, int64_t ldq,
+                           const double *__restrict__ alpha, double *__restrict__ X,
+                           double *__restrict__ R, T *__restrict__ S0, int64_t lds,
+                           float *__restrict__ R32, double *__restrict__ part) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int G = (m + 3) / 4, mp = G * 4;
+    T *As = reinterpret_cast<T *>(smem_raw);  // k x mp
+    double *red = reinterpret_cast<double *>(As + (size_t)k * mp +
+                                             ((size_t)k * mp * sizeof(T) % 16 ? 2 : 0));
+    for (int idx = threadIdx.x; idx < k * mp; idx += blockDim.x) {
+        int j = idx / mp, c = idx % mp;
+        As[idx] = c < m ? T(alpha[(size_t)j * m + c]) : T(0);
+    }
+    __syncthreads();
+    const int rows_per_block = blockDim.x / G;
+    const int lr = threadIdx.x / G, g = threadIdx.x % G;
+    const bool active = lr < rows_per_block;
+    double sq[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int64_t row = (int64_t)blockIdx.x * rows_per_block + lr; active && row < n;
+         row += (int64_t)gridDim.x * rows_per_block) {
+        T ax[4] = {T(0), T(0), T(0), T(0)}, ar[4] = {T(0), T(0), T(0), T(0)};
+        const T *qr = Q + row * ldq, *aqr = AQ + row * ldq;
+        for (int j = 0; j < k; j += 4) {
+            T q4[4], a4[4];
+            if constexpr (sizeof(T) == 4) {
+                float4 v = __ldg(reinterpret_cast<const float4 *>(qr + j));
+                float4 w = __ldg(reinterpret_cast<const float4 *>(aqr + j));
+                q4[0] = v.x; q4[1] = v.y; q4[2] = v.z; q4[3] = v.w;
+                a4[0] = w.x; a4[1] = w.y; a4[2] = w.z; a4[3] = w.w;
+            } else {
+                double2 v0 = __ldg(reinterpret_cast<const double2 *>(qr + j));
+                double2 v1 = __ldg(reinterpret_cast<const double2 *>(qr + j + 2));
+                double2 w0 = __ldg(reinterpret_cast<const double2 *>(aqr + j));
+                double2 w1 = __ldg(reinterpret_cast<const double2 *>(aqr + j + 2));
+                q4[0] = v0.x; q4[1] = v0.y; q4[2] = v1.x; q4[3] = v1.y;
+                a4[0] = w0.x; a4[1] = w0.y; a4[2] = w1.x; a4[3] = w1.y;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const T *al = As + (size_t)(j + u) * mp + g * 4;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    ax[q] = fma(q4[u], al[q], ax[q]);
+                    ar[q] = fma(a4[u], al[q], ar[q]);
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int c = g * 4 + q;
+            if (c < m) {
+                double x = X[row * m + c] + (double)ax[q];
+                double rv = R[row * m + c] - (double)ar[q];
+                X[row * m + c] = x;
+                R[row * m + c] = rv;
+                if (S0) S0[row * lds + c] = (T)rv;
+                if (R32) R32[row * m + c] = (float)rv;
+                sq[q] = fma(rv, rv, sq[q]);
+            }
+        }
+    }
+    if (!part) return;
+    __syncthreads();
+    if (active)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) red[lr * mp + g * 4 + q] = sq[q];
+    __syncthreads();
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+        double t = 0.0;
+        for (int rr = 0; rr < rows_per_block; ++rr) t += red[rr * mp + c];
+        part[(size_t)blockIdx.x * m + c] = t;
+    }
+}
+
+template <typename T>
+static bool direct_ok(int k, int64_t ld, const void *a, const void *b) {
+    return k % 4 == 0 && ld % 4 == 0 && aligned16(a) && (!b || aligned16(b));
+}
+
+template <typename T>
+int launch_qupdate_direct(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo,
+                          const T *Qin, int64_t ldq, const T *S, int64_t lds,
+                          const double *beta) {
+    const int G = k / 4;
+    int threads = std::max(G, (256 / G) * G);
+    if (threads > 256) threads = G;  // G <= 256 here
+    const int groups_per_block = threads / G;
+    size_t smem = (size_t)k * k * sizeof(T);
+    static const bool attr = [] {
+        cudaFuncSetAttribute(qupdate_direct_kernel<T>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    int64_t ngroups = (n + kDqRows - 1) / kDqRows;
+    int64_t blocks = (ngroups + groups_per_block - 1) / groups_per_block;
+    int64_t cap = (int64_t)sm_count() * 8;
+    if (blocks > cap) blocks = cap;
+    qupdate_direct_kernel<T><<<(unsigned)blocks, threads, smem, st>>>(n, k, Qout, ldo, Qin, ldq, S,
+                                                                      lds, beta);
+    return check_launch();
+}
+
+constexpr int kXrMaxBlocks = 2048;  // norm partials per xrupdate launch (upper bound)
+
+template <typename T>
+int launch_xrupdate_direct(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,
+                           int64_t ldq, const double *alpha, double *X, double *R, T *S0,
+                           int64_t lds, float *R32, double *norms, double *ws) {
+    const int G = (m + 3) / 4, mp = G * 4;
+    if (G > 256) return CACG_ERR_ARG;
+    const int threads = (256 / G) * G;
+    const int rows_per_block = threads / G;
+    size_t smem = (size_t)k * mp * sizeof(T) + 16 + (size_t)rows_per_block * mp * 8;
+    if (smem > max_smem_optin()) return CACG_ERR_UNSUPPORTED;
+    static const bool attr = [] {
+        cudaFuncSetAttribute(xrupdate_direct_kernel<T>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    int64_t blocks = (n + rows_per_block - 1) / rows_per_block;
+    int64_t cap = std::min<int64_t>((int64_t)sm_count() * 8, kXrMaxBlocks);
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    xrupdate_direct_kernel<T><<<(unsigned)blocks, threads, smem, st>>>(
+        n, k, m, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms ? ws : nullptr);
+    int rc = check_launch();
+    if (rc != CACG_OK || !norms) return rc;
+    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, (int)blocks, m, norms);
+    return check_launch();
+}
 
 // ------------------------------------------------------ residual epilogue
 // After R = B - A X (launch_spmm): S0 = cast(R), R32 = (float)R, norm partials.
@@ -532,12 +894,22 @@ extern "C" int cacg_k_xrupdate(int32_t vtype, int64_t n, int32_t k, int32_t m, c
         cudaSuccess)
         return CACG_ERR_OOM;
     int rc;
+    // vtype | CACG_XR_EXACT selects the float-float product sums
+    const bool exact = (vtype & CACG_XR_EXACT) != 0;
+    vtype &= ~CACG_XR_EXACT;
     if (vtype == CACG_VAL_F64)
-        rc = launch_xrupdate<double>(st, n, k, m, (const double *)Q, (const double *)AQ, ldq,
-                                     alpha, X, R, (double *)S0, lds, nullptr, norms, ws);
+        rc = exact ? launch_xrupdate<double>(st, n, k, m, (const double *)Q, (const double *)AQ,
+                                             ldq, alpha, X, R, (double *)S0, lds, nullptr,
+                                             norms, ws)
+                   : launch_xrupdate_fast<double>(st, n, k, m, (const double *)Q,
+                                                  (const double *)AQ, ldq, alpha, X, R,
+                                                  (double *)S0, lds, nullptr, norms, ws);
     else if (vtype == CACG_VAL_F32)
-        rc = launch_xrupdate<float>(st, n, k, m, (const float *)Q, (const float *)AQ, ldq, alpha,
-                                    X, R, (float *)S0, lds, nullptr, norms, ws);
+        rc = exact ? launch_xrupdate<float>(st, n, k, m, (const float *)Q, (const float *)AQ, ldq,
+                                            alpha, X, R, (float *)S0, lds, nullptr, norms, ws)
+                   : launch_xrupdate_fast<float>(st, n, k, m, (const float *)Q,
+                                                 (const float *)AQ, ldq, alpha, X, R,
+                                                 (float *)S0, lds, nullptr, norms, ws);
     else
         rc = CACG_ERR_ARG;
     cudaFreeAsync(ws, st);

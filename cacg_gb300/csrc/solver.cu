@@ -147,7 +147,9 @@ static Layout layout(int64_t n, int m, int s, int prec, bool lanczos) {
     //        bnorm m, true norms m, bounds 2, scalars 16, status (int) 16
     L.small = align256(sizeof(double) * ((size_t)4 * k * k + (size_t)2 * k * m + 3 * (size_t)m +
                                          64));
-    L.gram = align256(gram_workspace_bytes(n, k, k + m));
+    L.gram = align256(std::max(gram_workspace_bytes(n, k, k + m),
+                               prec == CACG_MIXED ? gram_tc_workspace_bytes(n, k, k + m)
+                                                  : (size_t)0));
     L.norm = align256(norm_workspace_doubles(n, std::max(m, 2)) * sizeof(double) + 4096);
     L.lanczos = lanczos ? align256((size_t)3 * n * 8) : 0;
     size_t o = 0;
@@ -540,9 +542,8 @@ struct Solver {
             std::swap(b.Q, b.S);
         } else {
             prof.begin(CACG_PHASE_GRAM, dn * 2.0 * k * ees, 2.0 * dn * k * k);
-            int rc = launch_gram<T>(st, p.gram_variant, n, (const T *)b.AQ, k, k, (const T *)b.S,
-                                    k, k, nullptr, 0, 0, b.QtAS, k, nullptr, 0, b.gram_ws,
-                                    b.gram_ws_bytes);
+            int rc = gram<T>((const T *)b.AQ, k, (const T *)b.S, k, k, nullptr, 0, 0, b.QtAS, k,
+                             nullptr, 0);
             prof.end();
             if (rc) return rc;
             prof.begin(CACG_PHASE_LU, 16.0 * k * k, 2.0 * (double)k * k * k);
@@ -566,8 +567,7 @@ struct Solver {
         const T *Rp = prec == CACG_MIXED ? (const T *)(const void *)b.R32
                                          : (const T *)(const void *)b.R;
         prof.begin(CACG_PHASE_GRAM, dn * (2.0 * k + m) * ees, 2.0 * dn * k * (k + m));
-        rc = launch_gram<T>(st, p.gram_variant, n, Q, k, k, AQ, k, k, Rp, m, m, b.QtAQ, k, b.QtR,
-                            m, b.gram_ws, b.gram_ws_bytes);
+        rc = gram<T>(Q, k, AQ, k, k, Rp, m, m, b.QtAQ, k, b.QtR, m);
         prof.end();
         if (rc) return rc;
         prof.begin(CACG_PHASE_LU, 16.0 * k * k, (2.0 / 3.0) * k * k * k + 2.0 * k * k * m);
@@ -579,13 +579,37 @@ struct Solver {
         prof.begin(CACG_PHASE_XRUPDATE,
                    dn * (2.0 * k * ees + 32.0 * m + ees * m + (b.R32 ? 4.0 * m : 0.0)),
                    4.0 * dn * k * m);
-        rc = launch_xrupdate<T>(st, n, k, m, Q, AQ, k, b.alpha, X, b.R, (T *)b.S, k, b.R32,
-                                b.norms, b.norm_ws);
+        rc = xrupdate<T>(Q, AQ, X);
         prof.end();
         return rc;
     }
 
     double sa = 0, sb = 0;
+
+    // Gram with the variant for this precision: the mixed mode uses the
+    // tensor-core kernel unless a CUDA-core variant is requested.
+    template <typename T>
+    int gram(const T *Lm, int ka, const T *R1, int64_t ldr1, int kb1, const T *R2, int64_t ldr2,
+             int kb2, double *C1, int ldc1, double *C2, int ldc2) {
+        const int64_t n = A->n;
+        if constexpr (std::is_same<T, float>::value) {
+            if (p.gram_variant == CACG_GRAM_AUTO || p.gram_variant == CACG_GRAM_TC)
+                return launch_gram_tc(st, n, Lm, k, ka, R1, ldr1, kb1, R2, ldr2, kb2, C1, ldc1,
+                                      C2, ldc2, b.gram_ws, b.gram_ws_bytes);
+        }
+        int v = p.gram_variant == CACG_GRAM_TC ? CACG_GRAM_FMA : p.gram_variant;
+        return launch_gram<T>(st, v, n, Lm, k, ka, R1, ldr1, kb1, R2, ldr2, kb2, C1, ldc1, C2,
+                              ldc2, b.gram_ws, b.gram_ws_bytes);
+    }
+
+    template <typename T>
+    int xrupdate(const T *Q, const T *AQ, double *X) {
+        if (prec == CACG_MIXED && p.exact_updates)
+            return launch_xrupdate<T>(st, A->n, k, m, Q, AQ, k, b.alpha, X, b.R, (T *)b.S, k,
+                                      b.R32, b.norms, b.norm_ws);
+        return launch_xrupdate_fast<T>(st, A->n, k, m, Q, AQ, k, b.alpha, X, b.R, (T *)b.S, k,
+                                       b.R32, b.norms, b.norm_ws);
+    }
 
     int fetch_norms(int *status_out) {
         CACG_CUDA_TRY(cudaMemcpyAsync(h_pin, b.norms, m * sizeof(double),

@@ -59,9 +59,10 @@ class Params:
     maxit: int = 1000
     precision: str = "fp64"         # "fp64" | "mixed"
     rr_period: int = 5
-    gram: str = "auto"              # "auto" | "fma" | "dmma"
+    gram: str = "auto"              # "auto" | "fma" | "dmma" | "tc" (mixed only)
     lanczos_seed: int = 12345
     stream: int = 0
+    exact_updates: bool = False     # mixed: float-float X/R update products
 
     def to_c(self) -> L.CacgParams:
         p = L.CacgParams()
@@ -81,9 +82,11 @@ class Params:
         p.maxit = self.maxit
         p.precision = {"fp64": L.FP64, "mixed": L.MIXED}[self.precision]
         p.rr_period = self.rr_period
-        p.gram_variant = {"auto": L.GRAM_AUTO, "fma": L.GRAM_FMA, "dmma": L.GRAM_DMMA}[self.gram]
+        p.gram_variant = {"auto": L.GRAM_AUTO, "fma": L.GRAM_FMA, "dmma": L.GRAM_DMMA,
+                          "tc": L.GRAM_TC}[self.gram]
         p.lanczos_seed = self.lanczos_seed
         p.stream = self.stream or None
+        p.exact_updates = 1 if self.exact_updates else 0
         return p
 
 

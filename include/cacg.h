@@ -57,9 +57,13 @@ extern "C" {
 #define CACG_GRAM_AUTO 0
 #define CACG_GRAM_FMA 1  /* FP64 FMA pipe */
 #define CACG_GRAM_DMMA 2 /* FP64 tensor core (mma.sync m8n8k4 f64) */
+#define CACG_GRAM_TC 3   /* FP32 inputs on the bf16 tensor cores: three bf16 slices
+                            per value, six slice products, FP32 accumulation over
+                            256-row groups, FP64 across groups */
 
 #define CACG_VAL_F64 0
 #define CACG_VAL_F32 1
+#define CACG_XR_EXACT 16 /* or-ed into cacg_k_xrupdate's vtype: float-float sums */
 
 /* generators (cacg_gen_*) */
 #define CACG_GEN_LAPLACE2D_5PT 1
@@ -97,7 +101,9 @@ typedef struct cacg_params {
     uint64_t lanczos_seed;
     void *stream;         /* cudaStream_t, NULL = the library's own stream */
     int32_t use_graph;    /* capture the outer iteration in a CUDA graph */
-    int32_t reserved[7];
+    int32_t exact_updates; /* MIXED: X/R update products summed in float-float
+                              instead of FP32 FMAs */
+    int32_t reserved[6];
 } cacg_params;
 
 typedef struct cacg_result {

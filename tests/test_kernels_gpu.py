@@ -140,10 +140,13 @@ def test_qupdate(lib, torch_cuda, vt, n, k):
     assert relerr(host(dq), want) <= (1e-13 if vt == F64 else 3e-6)
 
 
-@pytest.mark.parametrize("vt", [F64, F32])
+@pytest.mark.parametrize("vt,exact", [(F64, False), (F64, True), (F32, False), (F32, True)])
 @pytest.mark.parametrize("n,k,m", [(10000, 64, 8), (20000, 96, 16), (777, 4, 1),
                                    (3000, 15, 5), (4000, 256, 32)])
-def test_xrupdate(lib, torch_cuda, vt, n, k, m):
+def test_xrupdate(lib, torch_cuda, vt, exact, n, k, m):
+    """FP64: FP64 products.  FP32 inputs: float-float sums (exact=True) are
+    FP64-accurate; the default FP32-FMA sums carry FP32 rounding of the
+    k-term products only (X and R themselves are updated in FP64)."""
     torch = torch_cuda
     dt = np.float64 if vt == F64 else np.float32
     Q = O.gen_rhs("normal", n, k, 1).astype(dt)
@@ -156,10 +159,10 @@ def test_xrupdate(lib, torch_cuda, vt, n, k, m):
     dQ, dAQ, dal, dX, dR = (dev(torch, a) for a in (Q, AQ, al, X, R))
     S0 = torch.zeros((n, k), dtype=torch.float64 if vt == F64 else torch.float32, device="cuda")
     norms = torch.zeros(m, dtype=torch.float64, device="cuda")
-    rc = lib.cacg_k_xrupdate(vt, n, k, m, ptr(dQ), ptr(dAQ), k, ptr(dal), ptr(dX), ptr(dR),
-                             ptr(S0), k, ptr(norms), None)
+    rc = lib.cacg_k_xrupdate(vt | (16 if exact else 0), n, k, m, ptr(dQ), ptr(dAQ), k,
+                             ptr(dal), ptr(dX), ptr(dR), ptr(S0), k, ptr(norms), None)
     assert rc == 0
-    tol = 1e-13 if vt == F64 else 1e-11
+    tol = 1e-13 if vt == F64 else (1e-11 if exact else 5e-6)
     assert relerr(host(dX), Xw) <= tol
     assert relerr(host(dR), Rw) <= tol
     Rg = host(dR)
@@ -211,3 +214,23 @@ def test_gerschgorin_exact(lib, torch_cuda, kind, N):
     got = host(out)
     # min/max of per-row sums: per-row sums are formed in the reference order
     assert np.allclose(got, want, rtol=1e-14, atol=0)
+
+
+@pytest.mark.parametrize("n,ka,kb1,kb2", [(100000, 96, 96, 16), (200000, 96, 96, 0),
+                                          (5000, 24, 24, 4), (40000, 64, 64, 8),
+                                          (30000, 128, 128, 32), (3001, 12, 12, 3), (33, 4, 4, 1)])
+def test_gram_tensor_core_bf16_slices(lib, torch_cuda, n, ka, kb1, kb2):
+    """FP32 inputs on the bf16 tensor cores (three slices, six products,
+    FP32 over 256-row groups, FP64 across): normwise within 4e-6 of the exact
+    FP64 Gram of the FP32 values (FP32 accumulation inside the tensor core)."""
+    torch = torch_cuda
+    L = O.gen_rhs("normal", n, ka, 4).astype(np.float32)
+    R1 = O.gen_rhs("normal", n, kb1, 5).astype(np.float32)
+    R2 = O.gen_rhs("normal", n, max(kb2, 1), 6).astype(np.float32)[:, :kb2]
+    want = O.port_gram(L.astype(np.float64), np.hstack([R1, R2]).astype(np.float64))
+    d = {k_: dev(torch, a) for k_, a in dict(L=L, R1=R1, R2=R2).items()}
+    C = torch.zeros((ka, kb1 + kb2), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_gram(F32, 3, n, ptr(d["L"]), ka, ka, ptr(d["R1"]), kb1, kb1,
+                         ptr(d["R2"]) if kb2 else None, max(kb2, 1), kb2, ptr(C), kb1 + kb2, None)
+    assert rc == 0
+    assert relerr(host(C), want) <= 4e-6

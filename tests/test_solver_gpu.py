@@ -127,3 +127,28 @@ def test_zero_rhs_column_reports_breakdown(lib):
     with pytest.raises(cg.CacgError) as e:
         cg.solve(rp, ci, v, B, s=4, tol=1e-8, maxit=50)
     assert e.value.code == -4
+
+
+def test_mixed_cuda_core_exact_variant(lib):
+    """Mixed mode with the float-float Gram and X/R update (no tensor cores)."""
+    rp, ci, v = cg.gen_matrix("st3d27", 20)
+    n = len(rp) - 1
+    B = cg.gen_rhs("uniform", n, 16, 2, -1.0, 1.0)
+    X, info = cg.solve(rp, ci, v, B, s=6, bounds=("given", 0.05, 52.0), tol=1e-8, maxit=300,
+                       precision="mixed", gram="fma", exact_updates=True)
+    assert info["status"] == 0
+    assert O.port_true_relres(rp, ci, v, B, X).max() <= 1e-8
+
+
+@pytest.mark.parametrize("kind,N,m,s", [("lap3d7", 32, 8, 8), ("lap2d", 96, 4, 4),
+                                        ("st3d27", 24, 5, 6)])
+def test_mixed_tensor_core_converges_like_fp64(lib, kind, N, m, s):
+    rp, ci, v = cg.gen_matrix(kind, N)
+    n = len(rp) - 1
+    B = cg.gen_rhs("normal", n, m, 7)
+    kw = dict(s=s, bounds="gerschgorin", tol=1e-8, maxit=500)
+    X64, i64 = cg.solve(rp, ci, v, B, precision="fp64", **kw)
+    X32, i32 = cg.solve(rp, ci, v, B, precision="mixed", **kw)
+    assert i32["status"] == 0 and i64["status"] == 0
+    assert O.port_true_relres(rp, ci, v, B, X32).max() <= 1e-8
+    assert i32["iterations"] <= i64["iterations"] + 3
