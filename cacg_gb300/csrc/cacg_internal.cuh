@@ -1,6 +1,7 @@
 // cacg_internal.cuh -- shared device/host helpers of libcacg.so (sm_103a).
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -17,6 +18,7 @@ extern std::atomic<int64_t> g_launches;
 enum : int {
     kStatusBreakdown = 1,  // zero / non-finite pivot in the small LU
     kStatusNonFinite = 2,  // NaN/Inf in a residual norm
+    kStatusTimeout = 4,    // a bounded device-side wait ran out
 };
 
 #define CACG_CUDA_TRY(expr)                                                  \
@@ -72,10 +74,62 @@ __device__ __forceinline__ void vstore(float *p, const float (&d)[4]) {
 
 inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
+// ------------------------------------------------------ bf16 slice planes
+// An FP32 block may carry three bf16 "slice planes" (same shape and row
+// stride, planes `plane` elements apart) with x == s1 + s2 + s3 exactly up to
+// FP32's 24 bits: s1 = bf16(x), s2 = bf16(x - s1), s3 = bf16(x - s1 - s2).
+// Producers write them next to the FP32 value; the tensor-core Gram reads them.
+struct Slices {
+    __nv_bfloat16 *p = nullptr;  // plane 0; planes 1, 2 at +plane, +2*plane
+    int64_t plane = 0;
+};
+
+__device__ __forceinline__ void split3_bits(float x, unsigned short &h, unsigned short &m,
+                                            unsigned short &l) {
+    __nv_bfloat16 bh = __float2bfloat16_rn(x);
+    float r1 = x - __bfloat162float(bh);
+    __nv_bfloat16 bm = __float2bfloat16_rn(r1);
+    float r2 = r1 - __bfloat162float(bm);
+    __nv_bfloat16 bl = __float2bfloat16_rn(r2);
+    h = __bfloat16_as_ushort(bh);
+    m = __bfloat16_as_ushort(bm);
+    l = __bfloat16_as_ushort(bl);
+}
+
+// slices of one value at element offset `off`
+__device__ __forceinline__ void store_slices1(const Slices &S, int64_t off, float x) {
+    unsigned short h, m, l;
+    split3_bits(x, h, m, l);
+    unsigned short *b = reinterpret_cast<unsigned short *>(S.p);
+    b[off] = h;
+    b[S.plane + off] = m;
+    b[2 * S.plane + off] = l;
+}
+
+// slices of four consecutive values at an 8-byte-aligned element offset
+__device__ __forceinline__ void store_slices4(const Slices &S, int64_t off, const float (&x)[4]) {
+    unsigned short h[4], m[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) split3_bits(x[q], h[q], m[q], l[q]);
+    unsigned short *b = reinterpret_cast<unsigned short *>(S.p);
+    *reinterpret_cast<uint2 *>(b + off) =
+        make_uint2(h[0] | ((unsigned)h[1] << 16), h[2] | ((unsigned)h[3] << 16));
+    *reinterpret_cast<uint2 *>(b + S.plane + off) =
+        make_uint2(m[0] | ((unsigned)m[1] << 16), m[2] | ((unsigned)m[3] << 16));
+    *reinterpret_cast<uint2 *>(b + 2 * S.plane + off) =
+        make_uint2(l[0] | ((unsigned)l[1] << 16), l[2] | ((unsigned)l[3] << 16));
+}
+
 // ------------------------------------------------- launcher declarations
 // All launchers return CACG_OK or CACG_ERR_*; they are asynchronous.
 
-// Y = ca*(A X) + cb*Z1 + cc*Z2, width w (T = double / float).
+// Y = ca*(A X) + cb*Z1 + cc*Z2, width w (T = double / float); for float Y may
+// also get its bf16 slice planes (Ysl.p != nullptr).
+template <typename T>
+int launch_spmm_sl(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
+                   const T *val, int w, const T *X, int64_t ldx, T *Y, int64_t ldy,
+                   const T *Z1, int64_t ldz1, const T *Z2, int64_t ldz2, double ca, double cb,
+                   double cc, double avg_nnz, Slices Ysl);
 template <typename T>
 int launch_spmm(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
                 const T *val, int w, const T *X, int64_t ldx, T *Y, int64_t ldy,
@@ -88,6 +142,11 @@ int launch_residual(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t
                     const double *val, int m, const double *X, const double *B,
                     double *R, void *S0, int s0_is_f32, int64_t lds, double *norms,
                     double *ws, double avg_nnz);
+// Residual for the mixed mode: also R32 = (float)R and the slice planes of S0, R32.
+int launch_residual_sl(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
+                       const double *val, int m, const double *X, const double *B, double *R,
+                       float *S0, int64_t lds, float *R32, double *norms, double *ws,
+                       double avg_nnz, Slices S0sl, Slices R32sl);
 
 // Gram: C (ka x (kb1+kb2)) = L^T [R1 | R2] (FP64 accumulation).
 template <typename T>
@@ -102,11 +161,32 @@ int launch_gram_tc(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int 
                    const float *R1, int64_t ldr1, int kb1, const float *R2, int64_t ldr2, int kb2,
                    double *C1, int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes);
 size_t gram_tc_workspace_bytes(int64_t n, int ka, int kb);
+// Tensor-core Gram reading precomputed slice planes (L, R1, R2 slices; the
+// row strides ldl, ldr1, ldr2 and ka, kb1, kb2 multiples of 8).
+int launch_gram_tcs(cudaStream_t st, int64_t n, Slices L, int64_t ldl, int ka, Slices R1,
+                    int64_t ldr1, int kb1, Slices R2, int64_t ldr2, int kb2, double *C1,
+                    int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes);
+size_t gram_tcs_workspace_bytes(int64_t n, int ka, int kb);
+// tcgen05 Gram of FP32 blocks (bf16 slices converted in the kernel, TMEM
+// accumulators); *status gets kStatusTimeout if a bounded wait expires.
+int launch_gram_tc5(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int ka,
+                    const float *R1, int64_t ldr1, int kb1, const float *R2, int64_t ldr2,
+                    int kb2, double *C1, int ldc1, double *C2, int ldc2, double *ws,
+                    size_t ws_bytes, int *status);
+size_t gram_tc5_workspace_bytes(int64_t n, int ka, int kb);
+bool gram_tc5_supported(int ka, int kb);
+int launch_split_planes(cudaStream_t st, int64_t n, int w, const float *X, int64_t ld,
+                        Slices out);
+bool gram_tcs_supported(int ka, int kb1, int kb2, int64_t ldl, int64_t ldr1, int64_t ldr2);
 
 // Q_out = S - Q_in * beta  (Q_out may alias S; never Q_in).
 template <typename T>
 int launch_qupdate(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo,
                    const T *Qin, int64_t ldq, const T *S, int64_t lds, const double *beta);
+// Same, also writing Qout's slice planes (float, direct-load shapes only).
+int launch_qupdate_sl(cudaStream_t st, int64_t n, int k, float *Qout, int64_t ldo,
+                      const float *Qin, int64_t ldq, const float *S, int64_t lds,
+                      const double *beta, Slices Qsl);
 
 // X += Q alpha; R -= AQ alpha; S0 = (T)R; R32 = (float)R; norms.
 template <typename T>
@@ -114,13 +194,18 @@ int launch_xrupdate(cudaStream_t st, int64_t n, int k, int m, const T *Q, const 
                     int64_t ldq, const double *alpha, double *X, double *R, T *S0,
                     int64_t lds, float *R32, double *norms, double *ws);
 size_t norm_workspace_doubles(int64_t n, int m);
+// FP32 X/R update writing the slice planes of the next T_0 (S0) and of R32.
+int launch_xrupdate_sl(cudaStream_t st, int64_t n, int k, int m, const float *Q,
+                       const float *AQ, int64_t ldq, const double *alpha, double *X, double *R,
+                       float *S0, int64_t lds, float *R32, double *norms, double *ws,
+                       Slices S0sl, Slices R32sl);
 // Same update with the k-term products accumulated in T (FP32 FMAs for float).
 template <typename T>
 int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,
                          int64_t ldq, const double *alpha, double *X, double *R, T *S0,
                          int64_t lds, float *R32, double *norms, double *ws);
 
-// Small LU (Crout, U unit diagonal, no pivoting).
+// Small LU (Crout, U unit diagonal, no pivoting); F holds k*k + k doubles.
 int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *status);
 int launch_lu_solve(cudaStream_t st, int k, const double *F, int r, const double *RHS,
                     double *Y);

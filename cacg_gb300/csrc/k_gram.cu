@@ -446,6 +446,51 @@ extern "C" int cacg_k_gram(int32_t vtype, int32_t variant, int64_t n, const void
                            void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (kb2 > 0 && !R2) return CACG_ERR_ARG;
+    if (variant == CACG_GRAM_TC5) {
+        if (vtype != CACG_VAL_F32) return CACG_ERR_ARG;
+        if (!gram_tc5_supported(ka, kb1 + kb2)) return CACG_ERR_UNSUPPORTED;
+        size_t wsb = gram_tc5_workspace_bytes(n, ka, kb1 + kb2);
+        char *buf = nullptr;
+        if (cudaMallocAsync((void **)&buf, wsb + 256, st) != cudaSuccess) return CACG_ERR_OOM;
+        int *status = (int *)(buf + wsb);
+        cudaMemsetAsync(status, 0, sizeof(int), st);
+        int rc = launch_gram_tc5(st, n, (const float *)L, ldl, ka, (const float *)R1, ldr1, kb1,
+                                 (const float *)R2, ldr2, kb2, C, ldc, C + kb1, ldc, (double *)buf,
+                                 wsb, status);
+        int hs = 0;
+        if (rc == CACG_OK) {
+            cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) rc = CACG_ERR_CUDA;
+        }
+        cudaFreeAsync(buf, st);
+        if (rc == CACG_OK && (hs & kStatusTimeout)) rc = CACG_ERR_TIMEOUT;
+        return rc;
+    }
+    if (variant == CACG_GRAM_TC_SLICES) {
+        // split the FP32 inputs into slice planes, then the slice-plane kernel
+        if (vtype != CACG_VAL_F32) return CACG_ERR_ARG;
+        const int kb = kb1 + kb2;
+        if (!gram_tcs_supported(ka, kb1, kb2, ldl, ldr1, ldr2)) return CACG_ERR_ARG;
+        const size_t pl_l = (size_t)n * ldl, pl_1 = (size_t)n * ldr1,
+                     pl_2 = kb2 > 0 ? (size_t)n * ldr2 : 0;
+        size_t wsb = gram_tcs_workspace_bytes(n, ka, kb);
+        size_t tot = ((3 * (pl_l + pl_1 + pl_2) * 2 + 255) / 256) * 256 + wsb + 256;
+        char *buf = nullptr;
+        if (cudaMallocAsync((void **)&buf, tot, st) != cudaSuccess) return CACG_ERR_OOM;
+        Slices sL{(__nv_bfloat16 *)buf, (int64_t)pl_l};
+        Slices s1{sL.p + 3 * pl_l, (int64_t)pl_1};
+        Slices s2{s1.p + 3 * pl_1, (int64_t)pl_2};
+        double *w = (double *)(buf + ((3 * (pl_l + pl_1 + pl_2) * 2 + 255) / 256) * 256);
+        int rc = launch_split_planes(st, n, ka, (const float *)L, ldl, sL);
+        if (rc == CACG_OK) rc = launch_split_planes(st, n, kb1, (const float *)R1, ldr1, s1);
+        if (rc == CACG_OK && kb2 > 0)
+            rc = launch_split_planes(st, n, kb2, (const float *)R2, ldr2, s2);
+        if (rc == CACG_OK)
+            rc = launch_gram_tcs(st, n, sL, ldl, ka, s1, ldr1, kb1, s2, ldr2, kb2, C, ldc, C + kb1,
+                                 ldc, w, wsb);
+        cudaFreeAsync(buf, st);
+        return rc;
+    }
     if (variant == CACG_GRAM_TC) {
         if (vtype != CACG_VAL_F32) return CACG_ERR_ARG;
         size_t wsb = gram_tc_workspace_bytes(n, ka, kb1 + kb2);

@@ -11,6 +11,8 @@
 // for alpha, and one iteration later for beta); here the factor of each
 // Q^T AQ is computed once and reused by both solves.
 //
+// The factor F is k*k + k doubles: the Crout factors, then the reciprocals
+// of L's diagonal (the reference multiplies by 1/L_ii, src/DLSsolvers.c:168).
 // A zero or non-finite pivot sets *status = 1 (CACG_ERR_BREAKDOWN at the
 // host) instead of trapping; the arithmetic continues as the reference's
 // does (inf/NaN propagate) and the host stops the iteration.
@@ -31,11 +33,20 @@ __global__ void __launch_bounds__(kLuThreads)
     for (int i = threadIdx.x; i < kk; i += blockDim.x) W[i] = M[i];
     __syncthreads();
     int bad = 0;
+    double *Dinv = F + (size_t)kk;  // reciprocals of L's diagonal, read by the solves
     for (int d = 0; d < k; ++d) {
-        const double piv = W[d * k + d];
-        if (threadIdx.x == 0 && (piv == 0.0 || !isfinite(piv))) bad = 1;
-        const double inv = 1.0 / piv;
-        for (int c = d + 1 + threadIdx.x; c < k; c += blockDim.x) W[d * k + c] *= inv;
+        // warp 0 scales the pivot row; one FP64 division per step
+        if (threadIdx.x < 32) {
+            double inv = 0.0;
+            if (threadIdx.x == 0) {
+                const double piv = W[d * k + d];
+                if (piv == 0.0 || !isfinite(piv)) bad = 1;
+                inv = 1.0 / piv;
+                Dinv[d] = inv;
+            }
+            inv = __shfl_sync(0xffffffffu, inv, 0);
+            for (int c = d + 1 + threadIdx.x; c < k; c += 32) W[d * k + c] *= inv;
+        }
         __syncthreads();
         const int t = k - d - 1;
         for (int q = threadIdx.x; q < t * t; q += blockDim.x) {
@@ -49,20 +60,21 @@ __global__ void __launch_bounds__(kLuThreads)
     if (threadIdx.x == 0 && bad && status) atomicOr(status, kStatusBreakdown);
 }
 
-// Y (k x r) from the factor F and RHS (k x r).  Each CTA solves RC columns;
-// TPC threads cooperate on one column's inner products.
-constexpr int kLuRC = 32;
-constexpr int kLuTPC = 8;
+// Y (k x r) from the factor F (k*k factors + k reciprocal diagonal) and RHS
+// (k x r).  Each CTA solves kLuRC columns with kLuTPC threads per column
+// splitting the inner products; many CTAs spread the FP64 work over SMs.
+constexpr int kLuRC = 8;    // right-hand-side columns per CTA
+constexpr int kLuTPC = 16;  // threads per column
 
 __global__ void __launch_bounds__(kLuRC * kLuTPC)
     lu_solve_kernel(int k, const double *__restrict__ F, int r, const double *__restrict__ RHS,
                     double *__restrict__ Y, int use_smem) {
     extern __shared__ __align__(16) double sm[];
     double *Fs = use_smem ? sm : nullptr;
-    double *Z = sm + (use_smem ? (size_t)k * k : 0);  // k x kLuRC
+    double *Z = sm + (use_smem ? (size_t)k * k + k : 0);  // k x kLuRC
     const double *Fm = use_smem ? Fs : F;
     if (use_smem)
-        for (int i = threadIdx.x; i < k * k; i += blockDim.x) Fs[i] = F[i];
+        for (int i = threadIdx.x; i < k * k + k; i += blockDim.x) Fs[i] = F[i];
     const int c0 = blockIdx.x * kLuRC;
     const int cl = threadIdx.x / kLuTPC, sub = threadIdx.x % kLuTPC;
     const int col = c0 + cl;
@@ -78,10 +90,7 @@ __global__ void __launch_bounds__(kLuRC * kLuTPC)
         for (int q = sub; q < i; q += kLuTPC) s = fma(Fm[i * k + q], Z[q * kLuRC + cl], s);
 #pragma unroll
         for (int o = kLuTPC / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kLuTPC);
-        if (sub == 0 && active) {
-            double inv = 1.0 / Fm[i * k + i];
-            Z[i * kLuRC + cl] = (Z[i * kLuRC + cl] - s) * inv;
-        }
+        if (sub == 0 && active) Z[i * kLuRC + cl] = (Z[i * kLuRC + cl] - s) * Fm[k * k + i];
         __syncthreads();
     }
     // backward: Y[i] = Z[i] - sum_{q>i} U[i][q] Y[q]   (U unit diagonal)
@@ -117,8 +126,9 @@ int launch_lu_solve(cudaStream_t st, int k, const double *F, int r, const double
                     double *Y) {
     if (k <= 0 || r <= 0) return CACG_ERR_ARG;
     size_t zbytes = (size_t)k * kLuRC * sizeof(double);
-    int use_smem = ((size_t)k * k * sizeof(double) + zbytes) <= max_smem_optin() - 1024;
-    size_t smem = zbytes + (use_smem ? (size_t)k * k * sizeof(double) : 0);
+    size_t fbytes = ((size_t)k * k + k) * sizeof(double);
+    int use_smem = (fbytes + zbytes) <= max_smem_optin() - 1024;
+    size_t smem = zbytes + (use_smem ? fbytes : 0);
     if (smem > max_smem_optin()) return CACG_ERR_UNSUPPORTED;
     static const bool attr = [] {
         cudaFuncSetAttribute(lu_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -139,7 +149,7 @@ extern "C" int cacg_k_lu(int32_t k, const double *M, int32_t r, const double *RH
                          int *status, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     double *F = nullptr;
-    if (cudaMallocAsync((void **)&F, (size_t)k * k * sizeof(double), st) != cudaSuccess)
+    if (cudaMallocAsync((void **)&F, ((size_t)k * k + k) * sizeof(double), st) != cudaSuccess)
         return CACG_ERR_OOM;
     int rc = launch_lu_factor(st, k, M, F, status);
     if (rc == CACG_OK) rc = launch_lu_solve(st, k, F, r, RHS, Y);

@@ -62,7 +62,8 @@ __global__ void __launch_bounds__(kSpmmThreads)
     spmm_rows_kernel(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
                      const T *__restrict__ val, int w, const T *__restrict__ X,
                      int64_t ldx, T *__restrict__ Y, int64_t ldy, const T *__restrict__ Z1,
-                     int64_t ldz1, const T *__restrict__ Z2, int64_t ldz2, T ca, T cb, T cc) {
+                     int64_t ldz1, const T *__restrict__ Z2, int64_t ldz2, T ca, T cb, T cc,
+                     Slices ysl) {
     const int lt = threadIdx.x % TEAM;
     const int64_t team0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / TEAM;
     const int64_t nteams = ((int64_t)gridDim.x * blockDim.x) / TEAM;
@@ -135,6 +136,15 @@ __global__ void __launch_bounds__(kSpmmThreads)
                     for (int q = 0; q < CH; ++q) y[q] = fma(cc, z[q], y[q]);
                 }
                 store_chunk<T, CH>(Y + row * ldy + col, y);
+                if constexpr (sizeof(T) == 4) {
+                    if (ysl.p) {
+                        if constexpr (CH == 4)
+                            store_slices4(ysl, row * ldy + col, y);
+                        else
+#pragma unroll
+                            for (int q = 0; q < CH; ++q) store_slices1(ysl, row * ldy + col + q, y[q]);
+                    }
+                }
             }
         }
     }
@@ -186,11 +196,11 @@ template <typename T, int CH, int TEAM, int NCH>
 static int launch_rows(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
                        const T *val, int w, int ycols, const T *X, int64_t ldx, T *Y,
                        int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2, int64_t ldz2, T ca,
-                       T cb, T cc) {
+                       T cb, T cc, Slices ysl) {
     const int rows_per_block = kSpmmThreads / TEAM;
     dim3 grid(grid_for(n, rows_per_block), ycols);
     spmm_rows_kernel<T, CH, TEAM, NCH><<<grid, kSpmmThreads, 0, st>>>(
-        n, rp, ci, val, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc);
+        n, rp, ci, val, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc, ysl);
     return check_launch();
 }
 
@@ -198,11 +208,11 @@ template <typename T, int CH, int NCH>
 static int dispatch_team(int team, cudaStream_t st, int64_t n, const int32_t *rp,
                          const int32_t *ci, const T *val, int w, int ycols, const T *X,
                          int64_t ldx, T *Y, int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2,
-                         int64_t ldz2, T ca, T cb, T cc) {
+                         int64_t ldz2, T ca, T cb, T cc, Slices ysl) {
 #define CACG_TEAM_CASE(TM)                                                                \
     case TM:                                                                              \
         return launch_rows<T, CH, TM, NCH>(st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1, \
-                                           ldz1, Z2, ldz2, ca, cb, cc);
+                                           ldz1, Z2, ldz2, ca, cb, cc, ysl);
     switch (team) {
         CACG_TEAM_CASE(1)
         CACG_TEAM_CASE(2)
@@ -219,20 +229,20 @@ template <typename T, int CH>
 static int dispatch_nch(int nch, int team, cudaStream_t st, int64_t n, const int32_t *rp,
                         const int32_t *ci, const T *val, int w, int ycols, const T *X,
                         int64_t ldx, T *Y, int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2,
-                        int64_t ldz2, T ca, T cb, T cc) {
+                        int64_t ldz2, T ca, T cb, T cc, Slices ysl) {
     switch (nch) {
     case 1:
         return dispatch_team<T, CH, 1>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
-                                       ldz1, Z2, ldz2, ca, cb, cc);
+                                       ldz1, Z2, ldz2, ca, cb, cc, ysl);
     case 2:
         return dispatch_team<T, CH, 2>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
-                                       ldz1, Z2, ldz2, ca, cb, cc);
+                                       ldz1, Z2, ldz2, ca, cb, cc, ysl);
     case 3:
         return dispatch_team<T, CH, 3>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
-                                       ldz1, Z2, ldz2, ca, cb, cc);
+                                       ldz1, Z2, ldz2, ca, cb, cc, ysl);
     default:
         return dispatch_team<T, CH, 4>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
-                                       ldz1, Z2, ldz2, ca, cb, cc);
+                                       ldz1, Z2, ldz2, ca, cb, cc, ysl);
     }
 }
 
@@ -241,7 +251,17 @@ int launch_spmm(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci
                 const T *val, int w, const T *X, int64_t ldx, T *Y, int64_t ldy,
                 const T *Z1, int64_t ldz1, const T *Z2, int64_t ldz2, double ca_,
                 double cb_, double cc_, double avg_nnz) {
+    return launch_spmm_sl<T>(st, n, rp, ci, val, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca_, cb_,
+                             cc_, avg_nnz, Slices());
+}
+
+template <typename T>
+int launch_spmm_sl(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
+                   const T *val, int w, const T *X, int64_t ldx, T *Y, int64_t ldy,
+                   const T *Z1, int64_t ldz1, const T *Z2, int64_t ldz2, double ca_,
+                   double cb_, double cc_, double avg_nnz, Slices ysl) {
     if (n <= 0) return CACG_OK;
+    if (ysl.p && (sizeof(T) != 4 || w == 1)) return CACG_ERR_ARG;
     if (w <= 0 || !rp || !ci || !val || !X || !Y) return CACG_ERR_ARG;
     const T ca = T(ca_), cb = T(cb_), cc = T(cc_);
     if (w == 1) {
@@ -288,11 +308,15 @@ int launch_spmm(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci
     int yc = ycols > 1 ? (chunks + best_team * kMaxNch - 1) / (best_team * kMaxNch) : 1;
     if (vec)
         return dispatch_nch<T, VN>(nch, best_team, st, n, rp, ci, val, w, yc, X, ldx, Y, ldy, Z1,
-                                   ldz1, Z2, ldz2, ca, cb, cc);
+                                   ldz1, Z2, ldz2, ca, cb, cc, ysl);
     return dispatch_nch<T, 1>(nch, best_team, st, n, rp, ci, val, w, yc, X, ldx, Y, ldy, Z1,
-                              ldz1, Z2, ldz2, ca, cb, cc);
+                              ldz1, Z2, ldz2, ca, cb, cc, ysl);
 }
 
+template int launch_spmm_sl<float>(cudaStream_t, int64_t, const int32_t *, const int32_t *,
+                                   const float *, int, const float *, int64_t, float *, int64_t,
+                                   const float *, int64_t, const float *, int64_t, double, double,
+                                   double, double, Slices);
 template int launch_spmm<double>(cudaStream_t, int64_t, const int32_t *, const int32_t *,
                                  const double *, int, const double *, int64_t, double *,
                                  int64_t, const double *, int64_t, const double *, int64_t,

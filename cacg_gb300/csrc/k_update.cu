@@ -29,7 +29,8 @@ static bool direct_ok(int k, int64_t ld, const void *a, const void *b);
 template <typename T>
 int launch_xrupdate_direct(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,
                            int64_t ldq, const double *alpha, double *X, double *R, T *S0,
-                           int64_t lds, float *R32, double *norms, double *ws);
+                           int64_t lds, float *R32, double *norms, double *ws, Slices s0sl,
+                           Slices r32sl);
 
 // --------------------------------------------------------------- qupdate
 // Qout[i][c] = S[i][c] - sum_j Qin[i][j] * W[j][c]; W = beta (k x k FP64)
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(512)
 template <typename T>
 int launch_qupdate_direct(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo,
                           const T *Qin, int64_t ldq, const T *S, int64_t lds,
-                          const double *beta);
+                          const double *beta, Slices qsl);
 
 template <typename T>
 int launch_qupdate(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo, const T *Qin,
@@ -109,7 +110,7 @@ int launch_qupdate(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo, cons
     if (k <= 0 || (const void *)Qout == (const void *)Qin) return CACG_ERR_ARG;
     if (k % 4 == 0 && k / 4 <= 256 && ldq % 4 == 0 && (size_t)k * k * sizeof(T) <= 160 * 1024 &&
         aligned16(Qin))
-        return launch_qupdate_direct<T>(st, n, k, Qout, ldo, Qin, ldq, S, lds, beta);
+        return launch_qupdate_direct<T>(st, n, k, Qout, ldo, Qin, ldq, S, lds, beta, Slices());
     constexpr int TRP = kQuTR + 16 / sizeof(T);
     size_t budget = max_smem_optin() - 1024;
     auto need = [&](int bc) { return ((size_t)k * bc + (size_t)k * TRP) * sizeof(T); };
@@ -382,7 +383,7 @@ int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, c
     if (norms && !ws) return CACG_ERR_ARG;
     if (direct_ok<T>(k, ldq, Q, AQ))
         return launch_xrupdate_direct<T>(st, n, k, m, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms,
-                                         ws);
+                                         ws, Slices(), Slices());
     const int G = (m + kXrG - 1) / kXrG;
     if (G > kRowThreads) return CACG_ERR_ARG;
     const int mp = G * kXrG;
@@ -428,7 +429,8 @@ constexpr int kDqRows = 4;
 template <typename T>
 __global__ void __launch_bounds__(256)
     qupdate_direct_kernel(int64_t n, int k, T *Qout, int64_t ldo, const T *__restrict__ Qin,
-                          int64_t ldq, const T *S, int64_t lds, const double *__restrict__ beta) {
+                          int64_t ldq, const T *S, int64_t lds, const double *__restrict__ beta,
+                          Slices qsl) {
     // Qout may alias S (each element is read, then written, by one thread)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *Ws = reinterpret_cast<T *>(smem_raw);  // k x k
@@ -488,11 +490,14 @@ __global__ void __launch_bounds__(256)
             if (row >= n) break;
             const T *sp = S + row * lds + cg * 4;
             T *op = Qout + row * ldo + cg * 4;
-            T s0 = sp[0], s1 = sp[1], s2 = sp[2], s3 = sp[3];
-            op[0] = s0 - acc[i][0];
-            op[1] = s1 - acc[i][1];
-            op[2] = s2 - acc[i][2];
-            op[3] = s3 - acc[i][3];
+            T o[4] = {sp[0] - acc[i][0], sp[1] - acc[i][1], sp[2] - acc[i][2], sp[3] - acc[i][3]};
+            op[0] = o[0];
+            op[1] = o[1];
+            op[2] = o[2];
+            op[3] = o[3];
+            if constexpr (sizeof(T) == 4) {
+                if (qsl.p) store_slices4(qsl, row * ldo + cg * 4, o);
+            }
         }
     }
 }
@@ -505,7 +510,8 @@ __global__ void __launch_bounds__(256)
                            const T *__restrict__ AQ, int64_t ldq,
                            const double *__restrict__ alpha, double *__restrict__ X,
                            double *__restrict__ R, T *__restrict__ S0, int64_t lds,
-                           float *__restrict__ R32, double *__restrict__ part) {
+                           float *__restrict__ R32, double *__restrict__ part, Slices s0sl,
+                           Slices r32sl) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int G = (m + 3) / 4, mp = G * 4;
     T *As = reinterpret_cast<T *>(smem_raw);  // k x mp
@@ -549,6 +555,7 @@ __global__ void __launch_bounds__(256)
                 }
             }
         }
+        float rf[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int c = g * 4 + q;
@@ -559,9 +566,13 @@ __global__ void __launch_bounds__(256)
                 R[row * m + c] = rv;
                 if (S0) S0[row * lds + c] = (T)rv;
                 if (R32) R32[row * m + c] = (float)rv;
+                rf[q] = (float)rv;
                 sq[q] = fma(rv, rv, sq[q]);
             }
         }
+        // slice planes (used only with m % 4 == 0, so the group is full)
+        if (s0sl.p) store_slices4(s0sl, row * lds + g * 4, rf);
+        if (r32sl.p) store_slices4(r32sl, row * m + g * 4, rf);
     }
     if (!part) return;
     __syncthreads();
@@ -584,7 +595,7 @@ static bool direct_ok(int k, int64_t ld, const void *a, const void *b) {
 template <typename T>
 int launch_qupdate_direct(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo,
                           const T *Qin, int64_t ldq, const T *S, int64_t lds,
-                          const double *beta) {
+                          const double *beta, Slices qsl) {
     const int G = k / 4;
     int threads = std::max(G, (256 / G) * G);
     if (threads > 256) threads = G;  // G <= 256 here
@@ -601,7 +612,7 @@ int launch_qupdate_direct(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ld
     int64_t cap = (int64_t)sm_count() * 8;
     if (blocks > cap) blocks = cap;
     qupdate_direct_kernel<T><<<(unsigned)blocks, threads, smem, st>>>(n, k, Qout, ldo, Qin, ldq, S,
-                                                                      lds, beta);
+                                                                      lds, beta, qsl);
     return check_launch();
 }
 
@@ -610,7 +621,8 @@ constexpr int kXrMaxBlocks = 2048;  // norm partials per xrupdate launch (upper 
 template <typename T>
 int launch_xrupdate_direct(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,
                            int64_t ldq, const double *alpha, double *X, double *R, T *S0,
-                           int64_t lds, float *R32, double *norms, double *ws) {
+                           int64_t lds, float *R32, double *norms, double *ws, Slices s0sl,
+                           Slices r32sl) {
     const int G = (m + 3) / 4, mp = G * 4;
     if (G > 256) return CACG_ERR_ARG;
     const int threads = (256 / G) * G;
@@ -628,7 +640,7 @@ int launch_xrupdate_direct(cudaStream_t st, int64_t n, int k, int m, const T *Q,
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     xrupdate_direct_kernel<T><<<(unsigned)blocks, threads, smem, st>>>(
-        n, k, m, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms ? ws : nullptr);
+        n, k, m, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms ? ws : nullptr, s0sl, r32sl);
     int rc = check_launch();
     if (rc != CACG_OK || !norms) return rc;
     colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, (int)blocks, m, norms);
@@ -640,7 +652,8 @@ int launch_xrupdate_direct(cudaStream_t st, int64_t n, int k, int m, const T *Q,
 template <typename T>
 __global__ void __launch_bounds__(kRowThreads)
     rowpost_kernel(int64_t n, int m, int mp, const double *__restrict__ R, T *__restrict__ S0,
-                   int64_t lds, float *__restrict__ R32, double *__restrict__ part) {
+                   int64_t lds, float *__restrict__ R32, double *__restrict__ part,
+                   Slices s0sl = Slices(), Slices r32sl = Slices()) {
     __shared__ double red[kRowThreads];
     const int rows = blockDim.x / mp;
     const int r = threadIdx.x / mp, c = threadIdx.x % mp;
@@ -652,6 +665,8 @@ __global__ void __launch_bounds__(kRowThreads)
             double v = R[row * m + c];
             if (S0) S0[row * lds + c] = (T)v;
             if (R32) R32[row * m + c] = (float)v;
+            if (s0sl.p) store_slices1(s0sl, row * lds + c, (float)v);
+            if (r32sl.p) store_slices1(r32sl, row * m + c, (float)v);
             sq = fma(v, v, sq);
         }
     }
@@ -702,6 +717,47 @@ int launch_colnorm(cudaStream_t st, int64_t n, int m, const double *R, double *n
     if (rc != CACG_OK) return rc;
     colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G, m, norms);
     return check_launch();
+}
+
+int launch_residual_sl(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
+                       const double *val, int m, const double *X, const double *B, double *R,
+                       float *S0, int64_t lds, float *R32, double *norms, double *ws,
+                       double avg_nnz, Slices S0sl, Slices R32sl) {
+    int rc = launch_spmm<double>(st, n, rp, ci, val, m, X, m, R, m, B, m, nullptr, 0, -1.0,
+                                 1.0, 0.0, avg_nnz);
+    if (rc != CACG_OK) return rc;
+    if (m > kRowThreads) return CACG_ERR_ARG;
+    int mp = pow2ceil(m);
+    int rows = kRowThreads / mp;
+    int G = kRedBlocks;
+    int64_t tiles = (n + rows - 1) / rows;
+    if (tiles < G) G = (int)(tiles > 0 ? tiles : 1);
+    rowpost_kernel<float><<<G, kRowThreads, 0, st>>>(n, m, mp, R, S0, lds, R32,
+                                                     norms ? ws : nullptr, S0sl, R32sl);
+    rc = check_launch();
+    if (rc != CACG_OK || !norms) return rc;
+    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G, m, norms);
+    return check_launch();
+}
+
+int launch_qupdate_sl(cudaStream_t st, int64_t n, int k, float *Qout, int64_t ldo,
+                      const float *Qin, int64_t ldq, const float *S, int64_t lds,
+                      const double *beta, Slices Qsl) {
+    if (n <= 0) return CACG_OK;
+    if (!(k % 4 == 0 && k / 4 <= 256 && ldq % 4 == 0 && ldo % 4 == 0 &&
+          (size_t)k * k * sizeof(float) <= 160 * 1024 && aligned16(Qin)) ||
+        (const void *)Qout == (const void *)Qin)
+        return CACG_ERR_ARG;
+    return launch_qupdate_direct<float>(st, n, k, Qout, ldo, Qin, ldq, S, lds, beta, Qsl);
+}
+
+int launch_xrupdate_sl(cudaStream_t st, int64_t n, int k, int m, const float *Q,
+                       const float *AQ, int64_t ldq, const double *alpha, double *X, double *R,
+                       float *S0, int64_t lds, float *R32, double *norms, double *ws,
+                       Slices S0sl, Slices R32sl) {
+    if (m % 4 != 0 || !direct_ok<float>(k, ldq, Q, AQ) || (norms && !ws)) return CACG_ERR_ARG;
+    return launch_xrupdate_direct<float>(st, n, k, m, Q, AQ, ldq, alpha, X, R, S0, lds, R32,
+                                         norms, ws, S0sl, R32sl);
 }
 
 // ------------------------------------------------------------ Gerschgorin

@@ -134,22 +134,39 @@ static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 struct Layout {
     size_t S, Q, AQ, R, R32, Bnorm, small, gram, norm, lanczos, total;
     size_t o_S, o_Q, o_AQ, o_R, o_R32, o_small, o_gram, o_norm, o_lanczos;
+    size_t Ssl, R32sl, o_Ssl, o_Qsl, o_AQsl, o_R32sl;
+    bool slices;
 };
 
-static Layout layout(int64_t n, int m, int s, int prec, bool lanczos) {
+// With gram_variant CACG_GRAM_TC_SLICES the mixed mode carries bf16 slice
+// planes of S, Q, AQ and R32, written by their producers and read by the
+// tensor-core Gram (needs 16-byte slice rows: m a multiple of 8).
+static bool use_slice_planes(int m, int s, int prec, int gram_variant, int exact_updates) {
+    const int k = s * m;
+    return prec == CACG_MIXED && gram_variant == CACG_GRAM_TC_SLICES && !exact_updates &&
+           m % 8 == 0 && (size_t)k * k * sizeof(float) <= 160 * 1024;
+}
+
+static Layout layout(int64_t n, int m, int s, int prec, bool lanczos, bool slices = false) {
     Layout L{};
     const int k = s * m;
     const size_t es = prec == CACG_MIXED ? 4 : 8;
+    L.slices = slices;
     L.S = L.Q = L.AQ = align256((size_t)n * k * es + 64);
     L.R = align256((size_t)n * m * 8);
     L.R32 = prec == CACG_MIXED ? align256((size_t)n * m * 4) : 0;
+    L.Ssl = slices ? align256((size_t)3 * n * k * 2) : 0;
+    L.R32sl = slices ? align256((size_t)3 * n * m * 2) : 0;
     // small: QtAS k*k, QtAQ k*k, QtR k*m, F k*k, alpha k*m, beta k*k, norms m,
     //        bnorm m, true norms m, bounds 2, scalars 16, status (int) 16
-    L.small = align256(sizeof(double) * ((size_t)4 * k * k + (size_t)2 * k * m + 3 * (size_t)m +
-                                         64));
-    L.gram = align256(std::max(gram_workspace_bytes(n, k, k + m),
-                               prec == CACG_MIXED ? gram_tc_workspace_bytes(n, k, k + m)
-                                                  : (size_t)0));
+    L.small = align256(sizeof(double) * ((size_t)4 * k * k + k + (size_t)2 * k * m +
+                                         3 * (size_t)m + 64));
+    L.gram = align256(std::max(
+        gram_workspace_bytes(n, k, k + m),
+        prec == CACG_MIXED ? std::max(std::max(gram_tc_workspace_bytes(n, k, k + m),
+                                               gram_tcs_workspace_bytes(n, k, k + m)),
+                                      gram_tc5_workspace_bytes(n, k, k + m))
+                           : (size_t)0));
     L.norm = align256(norm_workspace_doubles(n, std::max(m, 2)) * sizeof(double) + 4096);
     L.lanczos = lanczos ? align256((size_t)3 * n * 8) : 0;
     size_t o = 0;
@@ -162,12 +179,17 @@ static Layout layout(int64_t n, int m, int s, int prec, bool lanczos) {
     L.o_gram = o; o += L.gram;
     L.o_norm = o; o += L.norm;
     L.o_lanczos = o; o += L.lanczos;
+    L.o_Ssl = o; o += L.Ssl;
+    L.o_Qsl = o; o += L.Ssl;
+    L.o_AQsl = o; o += L.Ssl;
+    L.o_R32sl = o; o += L.R32sl;
     L.total = o;
     return L;
 }
 
 size_t solve_workspace_bytes(int64_t n, int m, int s, int prec, bool lanczos) {
-    return layout(n, m, s, prec, lanczos).total;
+    return layout(n, m, s, prec, lanczos, use_slice_planes(m, s, prec, CACG_GRAM_TC_SLICES, 0))
+        .total;
 }
 
 // A growable cache of one device workspace per thread-less use (the bench
@@ -341,6 +363,7 @@ struct SolveBuffers {
     size_t gram_ws_bytes;
     double *norm_ws;
     double *lz;  // 3 x n (Lanczos)
+    Slices Ssl, Qsl, AQsl, R32sl;  // bf16 slice planes (mixed mode, when enabled)
 };
 
 static void carve(char *base, const Layout &L, int m, int k, SolveBuffers *b) {
@@ -352,7 +375,7 @@ static void carve(char *base, const Layout &L, int m, int k, SolveBuffers *b) {
     double *sm = (double *)(base + L.o_small);
     b->QtAS = sm; sm += (size_t)k * k;
     b->QtAQ = sm; sm += (size_t)k * k;
-    b->F = sm; sm += (size_t)k * k;
+    b->F = sm; sm += (size_t)k * k + k;
     b->beta = sm; sm += (size_t)k * k;
     b->QtR = sm; sm += (size_t)k * m;
     b->alpha = sm; sm += (size_t)k * m;
@@ -366,6 +389,14 @@ static void carve(char *base, const Layout &L, int m, int k, SolveBuffers *b) {
     b->gram_ws_bytes = L.gram;
     b->norm_ws = (double *)(base + L.o_norm);
     b->lz = L.lanczos ? (double *)(base + L.o_lanczos) : nullptr;
+}
+
+static void carve_slices(char *base, const Layout &L, int64_t n, int m, int k, SolveBuffers *b) {
+    if (!L.slices) return;
+    b->Ssl = Slices{(__nv_bfloat16 *)(base + L.o_Ssl), n * k};
+    b->Qsl = Slices{(__nv_bfloat16 *)(base + L.o_Qsl), n * k};
+    b->AQsl = Slices{(__nv_bfloat16 *)(base + L.o_AQsl), n * k};
+    b->R32sl = Slices{(__nv_bfloat16 *)(base + L.o_R32sl), n * m};
 }
 
 // Symmetric tridiagonal eigenvalues (diag a[0..k), off b[1..k)) by bisection
@@ -509,18 +540,29 @@ struct Solver {
 
     // R = B - A X (FP64); S0 = cast(R); R32; norms.  Used at start and for
     // residual replacement / true-residual checks.
+    bool slices = false;
+
     int residual(const double *B, const double *X, double *R, bool write_s0, double *norms) {
         const double dn = (double)A->n;
         prof.begin(CACG_PHASE_RESIDUAL,
                    (double)A->nnz * 12.0 + 4.0 * (dn + 1) + dn * m * (8.0 * 3 + (double)es()),
                    2.0 * (double)A->nnz * m);
-        int rc = launch_residual(st, A->n, A->rp, A->ci, A->val, m, X, B, R,
+        int rc;
+        if (slices && write_s0) {
+            rc = launch_residual_sl(st, A->n, A->rp, A->ci, A->val, m, X, B, R, (float *)b.S, k,
+                                    b.R32, norms, b.norm_ws, avg_nnz, b.Ssl, b.R32sl);
+        } else {
+            rc = launch_residual(st, A->n, A->rp, A->ci, A->val, m, X, B, R,
                                  write_s0 ? b.S : nullptr, prec == CACG_MIXED, k, norms,
                                  b.norm_ws, avg_nnz);
-        if (rc == CACG_OK && write_s0 && b.R32) rc = launch_cast_f64_f32(st, A->n * m, R, b.R32);
+            if (rc == CACG_OK && write_s0 && b.R32)
+                rc = launch_cast_f64_f32(st, A->n * m, R, b.R32);
+        }
         prof.end();
         return rc;
     }
+
+    static Slices at(Slices S, int64_t off) { return Slices{S.p ? S.p + off : nullptr, S.plane}; }
 
     template <typename T>
     int iterate_once(int it, double *X) {
@@ -534,15 +576,28 @@ struct Solver {
             double ca = j == 1 ? sa : 2.0 * sa, cb = j == 1 ? sb : 2.0 * sb;
             prof.begin(CACG_PHASE_BASIS, spmm_bytes(m, j >= 2 ? 1 : 0),
                        2.0 * (double)A->nnz * m + 5.0 * dn * m);
-            int rc = spmm<T>(Tm1, k, S + (size_t)j * m, k, m, Tm1, k, Tm2, k, ca, cb, -1.0);
+            int rc;
+            if constexpr (std::is_same<T, float>::value) {
+                rc = launch_spmm_sl<float>(st, n, A->rp, A->ci, A->val32, m, Tm1, k,
+                                           S + (size_t)j * m, k, Tm1, k, Tm2, k, ca, cb, -1.0,
+                                           avg_nnz, at(b.Ssl, (int64_t)j * m));
+            } else {
+                rc = spmm<T>(Tm1, k, S + (size_t)j * m, k, m, Tm1, k, Tm2, k, ca, cb, -1.0);
+            }
             prof.end();
             if (rc) return rc;
         }
         if (it == 0) {
             std::swap(b.Q, b.S);
+            std::swap(b.Qsl, b.Ssl);
         } else {
             prof.begin(CACG_PHASE_GRAM, dn * 2.0 * k * ees, 2.0 * dn * k * k);
-            int rc = gram<T>((const T *)b.AQ, k, (const T *)b.S, k, k, nullptr, 0, 0, b.QtAS, k,
+            int rc;
+            if (slices)
+                rc = launch_gram_tcs(st, n, b.AQsl, k, k, b.Ssl, k, k, Slices(), 0, 0, b.QtAS, k,
+                                     nullptr, 0, b.gram_ws, b.gram_ws_bytes);
+            else
+                rc = gram<T>((const T *)b.AQ, k, (const T *)b.S, k, k, nullptr, 0, 0, b.QtAS, k,
                              nullptr, 0);
             prof.end();
             if (rc) return rc;
@@ -552,22 +607,41 @@ struct Solver {
             if (rc) return rc;
             // Q_new = S - Q_old beta, written over S; then S <-> Q
             prof.begin(CACG_PHASE_QUPDATE, 3.0 * dn * k * ees, 2.0 * dn * k * k);
-            rc = launch_qupdate<T>(st, n, k, (T *)b.S, k, (const T *)b.Q, k, (const T *)b.S, k,
-                                   b.beta);
+            if constexpr (std::is_same<T, float>::value) {
+                if (slices)
+                    rc = launch_qupdate_sl(st, n, k, (float *)b.S, k, (const float *)b.Q, k,
+                                           (const float *)b.S, k, b.beta, b.Ssl);
+                else
+                    rc = launch_qupdate<T>(st, n, k, (T *)b.S, k, (const T *)b.Q, k,
+                                           (const T *)b.S, k, b.beta);
+            } else {
+                rc = launch_qupdate<T>(st, n, k, (T *)b.S, k, (const T *)b.Q, k, (const T *)b.S,
+                                       k, b.beta);
+            }
             prof.end();
             if (rc) return rc;
             std::swap(b.Q, b.S);
+            std::swap(b.Qsl, b.Ssl);
         }
         const T *Q = (const T *)b.Q;
         T *AQ = (T *)b.AQ;
         prof.begin(CACG_PHASE_AQ, spmm_bytes(k, 0), 2.0 * (double)A->nnz * k);
-        int rc = spmm<T>(Q, k, AQ, k, k, nullptr, 0, nullptr, 0, 1.0, 0.0, 0.0);
+        int rc;
+        if constexpr (std::is_same<T, float>::value)
+            rc = launch_spmm_sl<float>(st, n, A->rp, A->ci, A->val32, k, Q, k, AQ, k, nullptr, 0,
+                                       nullptr, 0, 1.0, 0.0, 0.0, avg_nnz, b.AQsl);
+        else
+            rc = spmm<T>(Q, k, AQ, k, k, nullptr, 0, nullptr, 0, 1.0, 0.0, 0.0);
         prof.end();
         if (rc) return rc;
         const T *Rp = prec == CACG_MIXED ? (const T *)(const void *)b.R32
                                          : (const T *)(const void *)b.R;
         prof.begin(CACG_PHASE_GRAM, dn * (2.0 * k + m) * ees, 2.0 * dn * k * (k + m));
-        rc = gram<T>(Q, k, AQ, k, k, Rp, m, m, b.QtAQ, k, b.QtR, m);
+        if (slices)
+            rc = launch_gram_tcs(st, n, b.Qsl, k, k, b.AQsl, k, k, b.R32sl, m, m, b.QtAQ, k,
+                                 b.QtR, m, b.gram_ws, b.gram_ws_bytes);
+        else
+            rc = gram<T>(Q, k, AQ, k, k, Rp, m, m, b.QtAQ, k, b.QtR, m);
         prof.end();
         if (rc) return rc;
         prof.begin(CACG_PHASE_LU, 16.0 * k * k, (2.0 / 3.0) * k * k * k + 2.0 * k * k * m);
@@ -593,7 +667,12 @@ struct Solver {
              int kb2, double *C1, int ldc1, double *C2, int ldc2) {
         const int64_t n = A->n;
         if constexpr (std::is_same<T, float>::value) {
-            if (p.gram_variant == CACG_GRAM_AUTO || p.gram_variant == CACG_GRAM_TC)
+            if ((p.gram_variant == CACG_GRAM_AUTO || p.gram_variant == CACG_GRAM_TC5) &&
+                gram_tc5_supported(ka, kb1 + kb2))
+                return launch_gram_tc5(st, n, Lm, k, ka, R1, ldr1, kb1, R2, ldr2, kb2, C1, ldc1,
+                                       C2, ldc2, b.gram_ws, b.gram_ws_bytes, b.status);
+            if (p.gram_variant == CACG_GRAM_AUTO || p.gram_variant == CACG_GRAM_TC ||
+                p.gram_variant == CACG_GRAM_TC5)
                 return launch_gram_tc(st, n, Lm, k, ka, R1, ldr1, kb1, R2, ldr2, kb2, C1, ldc1,
                                       C2, ldc2, b.gram_ws, b.gram_ws_bytes);
         }
@@ -604,6 +683,11 @@ struct Solver {
 
     template <typename T>
     int xrupdate(const T *Q, const T *AQ, double *X) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (slices)
+                return launch_xrupdate_sl(st, A->n, k, m, Q, AQ, k, b.alpha, X, b.R, (float *)b.S,
+                                          k, b.R32, b.norms, b.norm_ws, b.Ssl, b.R32sl);
+        }
         if (prec == CACG_MIXED && p.exact_updates)
             return launch_xrupdate<T>(st, A->n, k, m, Q, AQ, k, b.alpha, X, b.R, (T *)b.S, k,
                                       b.R32, b.norms, b.norm_ws);
@@ -673,6 +757,10 @@ struct Solver {
             ++since_rr;
             res->iterations = it + 1;
             res->recurrence_norm0 = sqrt(std::max(h_pin[0], 0.0));
+            if (stv & kStatusTimeout) {
+                res->status = CACG_ERR_TIMEOUT;
+                return CACG_ERR_TIMEOUT;
+            }
             if (stv & kStatusBreakdown) {
                 res->status = CACG_ERR_BREAKDOWN;
                 return CACG_ERR_BREAKDOWN;
@@ -760,7 +848,9 @@ int solve_on_device(const DevMatrix *A, const double *B, double *X, int m,
     S.prof.st = S.st;
     if (S.prec == CACG_MIXED && !A->val32) return CACG_ERR_ARG;
     bool lz = p.bounds_mode == CACG_BOUNDS_LANCZOS;
-    Layout L = layout(A->n, m, p.s, p.precision, lz);
+    const bool sl = use_slice_planes(m, p.s, p.precision, p.gram_variant, p.exact_updates);
+    Layout L = layout(A->n, m, p.s, p.precision, lz, sl);
+    S.slices = sl;
     void *ws = ws_external;
     bool from_cache = false;
     if (ws) {
@@ -770,6 +860,7 @@ int solve_on_device(const DevMatrix *A, const double *B, double *X, int m,
         if (rc) return rc;
     }
     carve((char *)ws, L, m, S.k, &S.b);
+    carve_slices((char *)ws, L, A->n, m, S.k, &S.b);
     double *pin_host = pinned_scratch(sizeof(double) * (2 * (size_t)m + 64));
     if (!pin_host) {
         if (!ws_external) ws_release(ws, from_cache);

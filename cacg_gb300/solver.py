@@ -59,7 +59,7 @@ class Params:
     maxit: int = 1000
     precision: str = "fp64"         # "fp64" | "mixed"
     rr_period: int = 5
-    gram: str = "auto"              # "auto" | "fma" | "dmma" | "tc" (mixed only)
+    gram: str = "auto"              # "auto" | "fma" | "dmma" | "tc" | "tc_slices" | "tc5"
     lanczos_seed: int = 12345
     stream: int = 0
     exact_updates: bool = False     # mixed: float-float X/R update products
@@ -83,7 +83,8 @@ class Params:
         p.precision = {"fp64": L.FP64, "mixed": L.MIXED}[self.precision]
         p.rr_period = self.rr_period
         p.gram_variant = {"auto": L.GRAM_AUTO, "fma": L.GRAM_FMA, "dmma": L.GRAM_DMMA,
-                          "tc": L.GRAM_TC}[self.gram]
+                          "tc": L.GRAM_TC, "tc_slices": L.GRAM_TC_SLICES,
+                          "tc5": L.GRAM_TC5}[self.gram]
         p.lanczos_seed = self.lanczos_seed
         p.stream = self.stream or None
         p.exact_updates = 1 if self.exact_updates else 0

@@ -60,6 +60,10 @@ extern "C" {
 #define CACG_GRAM_TC 3   /* FP32 inputs on the bf16 tensor cores: three bf16 slices
                             per value, six slice products, FP32 accumulation over
                             256-row groups, FP64 across groups */
+#define CACG_GRAM_TC_SLICES 4 /* same products, from bf16 slice planes written by the
+                                 producers (cacg_k_gram splits its inputs first) */
+#define CACG_GRAM_TC5 5  /* same products on the 5th-generation tensor cores
+                            (tcgen05.mma, accumulator in tensor memory) */
 
 #define CACG_VAL_F64 0
 #define CACG_VAL_F32 1

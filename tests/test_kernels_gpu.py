@@ -216,21 +216,25 @@ def test_gerschgorin_exact(lib, torch_cuda, kind, N):
     assert np.allclose(got, want, rtol=1e-14, atol=0)
 
 
+@pytest.mark.parametrize("variant", [3, 4, 5])
 @pytest.mark.parametrize("n,ka,kb1,kb2", [(100000, 96, 96, 16), (200000, 96, 96, 0),
                                           (5000, 24, 24, 4), (40000, 64, 64, 8),
                                           (30000, 128, 128, 32), (3001, 12, 12, 3), (33, 4, 4, 1)])
-def test_gram_tensor_core_bf16_slices(lib, torch_cuda, n, ka, kb1, kb2):
+def test_gram_tensor_core_bf16_slices(lib, torch_cuda, variant, n, ka, kb1, kb2):
     """FP32 inputs on the bf16 tensor cores (three slices, six products,
     FP32 over 256-row groups, FP64 across): normwise within 4e-6 of the exact
     FP64 Gram of the FP32 values (FP32 accumulation inside the tensor core)."""
     torch = torch_cuda
+    if variant == 4 and (ka % 8 or kb1 % 8 or kb2 % 8):
+        pytest.skip("slice planes need widths that are multiples of 8")
     L = O.gen_rhs("normal", n, ka, 4).astype(np.float32)
     R1 = O.gen_rhs("normal", n, kb1, 5).astype(np.float32)
     R2 = O.gen_rhs("normal", n, max(kb2, 1), 6).astype(np.float32)[:, :kb2]
     want = O.port_gram(L.astype(np.float64), np.hstack([R1, R2]).astype(np.float64))
     d = {k_: dev(torch, a) for k_, a in dict(L=L, R1=R1, R2=R2).items()}
     C = torch.zeros((ka, kb1 + kb2), dtype=torch.float64, device="cuda")
-    rc = lib.cacg_k_gram(F32, 3, n, ptr(d["L"]), ka, ka, ptr(d["R1"]), kb1, kb1,
-                         ptr(d["R2"]) if kb2 else None, max(kb2, 1), kb2, ptr(C), kb1 + kb2, None)
+    rc = lib.cacg_k_gram(F32, variant, n, ptr(d["L"]), ka, ka, ptr(d["R1"]), kb1, kb1,
+                         ptr(d["R2"]) if kb2 else None, kb2 if kb2 else 8, kb2, ptr(C), kb1 + kb2,
+                         None)
     assert rc == 0
     assert relerr(host(C), want) <= 4e-6
