@@ -175,6 +175,11 @@ int launch_gram_tc5(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int
                     size_t ws_bytes, int *status);
 size_t gram_tc5_workspace_bytes(int64_t n, int ka, int kb);
 bool gram_tc5_supported(int ka, int kb);
+// Q_out = S - Q_in beta on tcgen05 (FP32 Q, S; FP64 beta), k % 16 == 0, k <= 96
+int launch_qupdate_tc5(cudaStream_t st, int64_t n, int k, float *Qout, int64_t ldo,
+                       const float *Qin, int64_t ldq, const float *S, int64_t lds,
+                       const double *beta, int *status);
+bool tsm_q_tc5_supported(int k);
 int launch_split_planes(cudaStream_t st, int64_t n, int w, const float *X, int64_t ld,
                         Slices out);
 bool gram_tcs_supported(int ka, int kb1, int kb2, int64_t ldl, int64_t ldr1, int64_t ldr2);

@@ -150,6 +150,180 @@ __global__ void __launch_bounds__(kSpmmThreads)
     }
 }
 
+// Warp-staged variant: warp w owns blocks of RPW = 32 / TEAM consecutive
+// rows (one row per team).  The column indices and values of a block are
+// copied into this warp's shared-memory buffer with 16-byte cp.async one block
+// ahead, and the block's row pointers are loaded two blocks ahead, so a row's
+// dependent chain is only the X gathers (mostly L1/L2 hits) instead of row
+// pointer -> index/value -> gather round trips to HBM.  A block with more
+// than `cap` staged entries is processed straight from global memory.
+// Requires 2 <= TEAM (RPW + 1 row pointers fit in the warp's lanes) and
+// 16-byte aligned ci / val.
+template <typename T, int CH, int NCH>
+__device__ __forceinline__ void ws_row(int64_t row, int lt, int TEAMv, int colbase, int w,
+                                       const int32_t *cis, const T *vs, int cnt,
+                                       const T *__restrict__ X, int64_t ldx, T (&acc)[NCH][CH]) {
+    int p = 0;
+    for (; p + kGroup <= cnt; p += kGroup) {
+        int cg[kGroup];
+        T ag[kGroup];
+#pragma unroll
+        for (int u = 0; u < kGroup; ++u) {
+            cg[u] = cis[p + u];
+            ag[u] = vs[p + u];
+        }
+#pragma unroll
+        for (int j = 0; j < NCH; ++j) {
+            const int col = (lt + j * TEAMv) * CH;
+            if (colbase + col < w) {
+                T x[kGroup][CH];
+#pragma unroll
+                for (int u = 0; u < kGroup; ++u)
+                    load_chunk<T, CH>(x[u], X + (int64_t)cg[u] * ldx + colbase + col);
+#pragma unroll
+                for (int u = 0; u < kGroup; ++u)
+#pragma unroll
+                    for (int q = 0; q < CH; ++q) acc[j][q] = fma(ag[u], x[u][q], acc[j][q]);
+            }
+        }
+    }
+    for (; p < cnt; ++p) {
+        const int c = cis[p];
+        const T a = vs[p];
+#pragma unroll
+        for (int j = 0; j < NCH; ++j) {
+            const int col = (lt + j * TEAMv) * CH;
+            if (colbase + col < w) {
+                T x[CH];
+                load_chunk<T, CH>(x, X + (int64_t)c * ldx + colbase + col);
+#pragma unroll
+                for (int q = 0; q < CH; ++q) acc[j][q] = fma(a, x[q], acc[j][q]);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void ws_cp16(void *smem, const void *g, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(smem)),
+                 "l"(g), "r"(bytes));
+}
+
+template <typename T, int CH, int TEAM, int NCH>
+__global__ void __launch_bounds__(kSpmmThreads)
+    spmm_ws_kernel(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                   const T *__restrict__ val, int cap, int w, const T *__restrict__ X,
+                   int64_t ldx, T *__restrict__ Y, int64_t ldy, const T *__restrict__ Z1,
+                   int64_t ldz1, const T *__restrict__ Z2, int64_t ldz2, T ca, T cb, T cc,
+                   Slices ysl) {
+    static_assert(TEAM >= 2 && TEAM <= 32, "RPW + 1 row pointers must fit in a warp");
+    constexpr int RPW = 32 / TEAM;
+    constexpr int VPC = 16 / (int)sizeof(T);  // values per 16-byte chunk
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    // this warp: ci[2][cap], val[2][cap]
+    int32_t *ci_s = reinterpret_cast<int32_t *>(smem_raw + (size_t)wib * 2 * cap * (4 + sizeof(T)));
+    T *val_s = reinterpret_cast<T *>(ci_s + 2 * cap);
+    const int lt = lane % TEAM, team = lane / TEAM;
+    const int colbase = blockIdx.y * (TEAM * NCH * CH);
+    const int64_t nblk = (n + RPW - 1) / RPW;
+    const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int nnz = __ldg(rp + n);
+
+    auto load_rp = [&](int64_t blk) -> int {  // lane l <= RPW: rp[blk * RPW + l] (clamped)
+        if (blk >= nblk || lane > RPW) return 0;
+        int64_t r = blk * RPW + lane;
+        return __ldg(rp + (r < n ? r : n));
+    };
+    auto stage = [&](int rpv, int64_t blk, int buf) {
+        if (blk < nblk) {
+            const int s = __shfl_sync(0xffffffffu, rpv, 0) & ~3;
+            const int e = (__shfl_sync(0xffffffffu, rpv, RPW) + 3) & ~3;
+            if (e - s <= cap) {
+                for (int c = lane; c < (e - s) / 4; c += 32) {
+                    const int g0 = s + 4 * c;
+                    const int by = max(0, min(16, (nnz - g0) * 4));
+                    ws_cp16(ci_s + buf * cap + 4 * c, by ? (const void *)(ci + g0) : ci, by);
+                }
+                for (int c = lane; c < (e - s) / VPC; c += 32) {
+                    const int g0 = s + VPC * c;
+                    const int by = max(0, min(16, (nnz - g0) * (int)sizeof(T)));
+                    ws_cp16(val_s + buf * cap + VPC * c, by ? (const void *)(val + g0) : val, by);
+                }
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::);
+    };
+
+    int64_t blk = wg;
+    int rp_cur = load_rp(blk);
+    stage(rp_cur, blk, 0);
+    int rp_next = load_rp(blk + nw);
+    int buf = 0;
+    for (; blk < nblk; blk += nw, buf ^= 1) {
+        stage(rp_next, blk + nw, buf ^ 1);
+        const int rp_after = load_rp(blk + 2 * nw);
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncwarp();
+        const int s = __shfl_sync(0xffffffffu, rp_cur, 0) & ~3;
+        const int e = (__shfl_sync(0xffffffffu, rp_cur, RPW) + 3) & ~3;
+        const bool staged = e - s <= cap;
+        const int rb = __shfl_sync(0xffffffffu, rp_cur, team);
+        const int re = __shfl_sync(0xffffffffu, rp_cur, team + 1);
+        const int64_t row = blk * RPW + team;
+        if (row < n) {
+            T acc[NCH][CH];
+#pragma unroll
+            for (int j = 0; j < NCH; ++j)
+#pragma unroll
+                for (int q = 0; q < CH; ++q) acc[j][q] = T(0);
+            if (staged)
+                ws_row<T, CH, NCH>(row, lt, TEAM, colbase, w, ci_s + buf * cap + (rb - s),
+                                   val_s + buf * cap + (rb - s), re - rb, X, ldx, acc);
+            else
+                ws_row<T, CH, NCH>(row, lt, TEAM, colbase, w, ci + rb, val + rb, re - rb, X, ldx,
+                                   acc);
+#pragma unroll
+            for (int j = 0; j < NCH; ++j) {
+                const int col = colbase + (lt + j * TEAM) * CH;
+                if (col < w) {
+                    T y[CH];
+#pragma unroll
+                    for (int q = 0; q < CH; ++q) y[q] = ca * acc[j][q];
+                    if (Z1) {
+                        T z[CH];
+                        load_chunk_plain<T, CH>(z, Z1 + row * ldz1 + col);
+#pragma unroll
+                        for (int q = 0; q < CH; ++q) y[q] = fma(cb, z[q], y[q]);
+                    }
+                    if (Z2) {
+                        T z[CH];
+                        load_chunk_plain<T, CH>(z, Z2 + row * ldz2 + col);
+#pragma unroll
+                        for (int q = 0; q < CH; ++q) y[q] = fma(cc, z[q], y[q]);
+                    }
+                    store_chunk<T, CH>(Y + row * ldy + col, y);
+                    if constexpr (sizeof(T) == 4) {
+                        if (ysl.p) {
+                            if constexpr (CH == 4)
+                                store_slices4(ysl, row * ldy + col, y);
+                            else
+#pragma unroll
+                                for (int q = 0; q < CH; ++q)
+                                    store_slices1(ysl, row * ldy + col + q, y[q]);
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();  // every lane is done with this buffer before it is refilled
+        rp_cur = rp_next;
+        rp_next = rp_after;
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // Single column: TEAM lanes split the nonzeros of a row, shuffle-reduce.
 template <typename T, int TEAM>
 __global__ void __launch_bounds__(kSpmmThreads)
@@ -196,8 +370,33 @@ template <typename T, int CH, int TEAM, int NCH>
 static int launch_rows(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
                        const T *val, int w, int ycols, const T *X, int64_t ldx, T *Y,
                        int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2, int64_t ldz2, T ca,
-                       T cb, T cc, Slices ysl) {
+                       T cb, T cc, Slices ysl, double avg_nnz) {
     const int rows_per_block = kSpmmThreads / TEAM;
+    if constexpr (TEAM >= 2) {
+        if (aligned16(ci) && aligned16(val) && avg_nnz > 0) {
+            // staged entries per warp buffer: RPW rows at 1.5x the mean row
+            // length (multiple of 4), plus alignment slack at both ends
+            constexpr int RPW = 32 / TEAM;
+            int per_row = ((int)(1.5 * avg_nnz) + 3) & ~3;
+            if (per_row < 8) per_row = 8;
+            int cap = RPW * per_row + 8;
+            const int warps = kSpmmThreads / 32;
+            const size_t max_smem = 96 * 1024;  // keep >= 2 blocks per SM
+            while (cap > 16 && (size_t)warps * 2 * cap * (4 + sizeof(T)) > max_smem) cap -= 4;
+            const size_t smem = (size_t)warps * 2 * cap * (4 + sizeof(T));
+            static const bool attr = [] {
+                cudaFuncSetAttribute(spmm_ws_kernel<T, CH, TEAM, NCH>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+                return true;
+            }();
+            (void)attr;
+            const int64_t nblk = (n + RPW - 1) / RPW;
+            dim3 grid(grid_for(nblk, warps), ycols);
+            spmm_ws_kernel<T, CH, TEAM, NCH><<<grid, kSpmmThreads, smem, st>>>(
+                n, rp, ci, val, cap, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc, ysl);
+            return check_launch();
+        }
+    }
     dim3 grid(grid_for(n, rows_per_block), ycols);
     spmm_rows_kernel<T, CH, TEAM, NCH><<<grid, kSpmmThreads, 0, st>>>(
         n, rp, ci, val, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc, ysl);
@@ -208,11 +407,11 @@ template <typename T, int CH, int NCH>
 static int dispatch_team(int team, cudaStream_t st, int64_t n, const int32_t *rp,
                          const int32_t *ci, const T *val, int w, int ycols, const T *X,
                          int64_t ldx, T *Y, int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2,
-                         int64_t ldz2, T ca, T cb, T cc, Slices ysl) {
+                         int64_t ldz2, T ca, T cb, T cc, Slices ysl, double avg_nnz) {
 #define CACG_TEAM_CASE(TM)                                                                \
     case TM:                                                                              \
         return launch_rows<T, CH, TM, NCH>(st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1, \
-                                           ldz1, Z2, ldz2, ca, cb, cc, ysl);
+                                           ldz1, Z2, ldz2, ca, cb, cc, ysl, avg_nnz);
     switch (team) {
         CACG_TEAM_CASE(1)
         CACG_TEAM_CASE(2)
@@ -229,20 +428,20 @@ template <typename T, int CH>
 static int dispatch_nch(int nch, int team, cudaStream_t st, int64_t n, const int32_t *rp,
                         const int32_t *ci, const T *val, int w, int ycols, const T *X,
                         int64_t ldx, T *Y, int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2,
-                        int64_t ldz2, T ca, T cb, T cc, Slices ysl) {
+                        int64_t ldz2, T ca, T cb, T cc, Slices ysl, double avg_nnz) {
     switch (nch) {
     case 1:
         return dispatch_team<T, CH, 1>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
-                                       ldz1, Z2, ldz2, ca, cb, cc, ysl);
+                                       ldz1, Z2, ldz2, ca, cb, cc, ysl, avg_nnz);
     case 2:
         return dispatch_team<T, CH, 2>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
-                                       ldz1, Z2, ldz2, ca, cb, cc, ysl);
+                                       ldz1, Z2, ldz2, ca, cb, cc, ysl, avg_nnz);
     case 3:
         return dispatch_team<T, CH, 3>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
-                                       ldz1, Z2, ldz2, ca, cb, cc, ysl);
+                                       ldz1, Z2, ldz2, ca, cb, cc, ysl, avg_nnz);
     default:
         return dispatch_team<T, CH, 4>(team, st, n, rp, ci, val, w, ycols, X, ldx, Y, ldy, Z1,
-                                       ldz1, Z2, ldz2, ca, cb, cc, ysl);
+                                       ldz1, Z2, ldz2, ca, cb, cc, ysl, avg_nnz);
     }
 }
 
@@ -308,9 +507,9 @@ int launch_spmm_sl(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t 
     int yc = ycols > 1 ? (chunks + best_team * kMaxNch - 1) / (best_team * kMaxNch) : 1;
     if (vec)
         return dispatch_nch<T, VN>(nch, best_team, st, n, rp, ci, val, w, yc, X, ldx, Y, ldy, Z1,
-                                   ldz1, Z2, ldz2, ca, cb, cc, ysl);
+                                   ldz1, Z2, ldz2, ca, cb, cc, ysl, avg_nnz);
     return dispatch_nch<T, 1>(nch, best_team, st, n, rp, ci, val, w, yc, X, ldx, Y, ldy, Z1,
-                              ldz1, Z2, ldz2, ca, cb, cc, ysl);
+                              ldz1, Z2, ldz2, ca, cb, cc, ysl, avg_nnz);
 }
 
 template int launch_spmm_sl<float>(cudaStream_t, int64_t, const int32_t *, const int32_t *,

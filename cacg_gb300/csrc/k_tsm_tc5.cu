@@ -1,0 +1,322 @@
+// k_tsm_tc5.cu -- tall-skinny x small products on the 5th-generation tensor
+// cores (tcgen05, sm_103a): the mixed-precision Q update
+//     Q_out = S - Q_in * beta      (Q_in, S: n x k FP32; beta: k x k FP64)
+//
+// Reference operations replaced (sclc/cacg): dense_distributedMatL_localMatR_Mul_v1
+// (src/BLAS3.c:794-825) forming Q*beta and dense_mat_mat_add_TP
+// (src/BLAS3.c:579-612) forming S - Q*beta, fused into one pass.
+//
+// Work split: persistent CTAs (one per SM) walk 128-row tiles of Q; a tile
+// is K = k columns deep, processed in steps of 32 columns.
+//   * warps 0-7 (producers) stream each step's 128 x 32 FP32 block of Q_in
+//     through a 4-stage cp.async ring (rows padded to 36 floats so the
+//     conversion reads are conflict-free) and split it into three bf16
+//     slices in the K-major core-matrix layout (8 rows x 16 bytes, LBO =
+//     128 B, SBO = 512 B); thread 0 issues the step's 12 MMAs (six slice
+//     products, two K = 16 halves) against beta's slices, which stay resident
+//     in shared memory for the whole launch (N = k rows, SBO = k/8 * 128 B);
+//   * the tile's FP32 accumulator (128 lanes x k columns) lives in one of two
+//     TMEM buffers; after the tile's last MMAs the issuer commits to that
+//     buffer's "full" mbarrier;
+//   * warps 8-11 (epilogue, one per TMEM lane quadrant) load their S row
+//     before the wait, then read the accumulator with tcgen05.ld, write
+//     S - acc to Q_out and release the buffer ("empty" mbarrier), so the
+//     epilogue of tile t overlaps the MMAs of tile t+1.
+// Products: six bf16 slice products of order <= 2^-16 (FP32-level products),
+// FP32 accumulation over K = k, as the CUDA-core kernel's FP32 FMA chain.
+// Every mbarrier wait is bounded; on expiry kStatusTimeout is recorded, the
+// producers leave together at their next named barrier, the epilogue warps
+// stop at the abort flag, the issuer waits (bounded) for its committed MMAs
+// and TMEM is freed.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "cacg_internal.cuh"
+#include "tc5_util.cuh"
+
+namespace cacg {
+
+constexpr int kTsM = 128;                     // rows per tile (UMMA M)
+constexpr int kTsKT = 32;                     // K columns per step
+constexpr int kTsStages = 4;                  // FP32 ring depth
+constexpr int kTsProd = 256;                  // producer threads (warps 0-7)
+constexpr int kTsEpi = 128;                   // epilogue threads (warps 8-11)
+constexpr int kTsThreads = kTsProd + kTsEpi;  // 12 warps
+constexpr int kTsRingLd = kTsKT + 4;          // padded ring row (floats)
+constexpr int kTsMaxNN = 6;                   // k <= 96: S row of the epilogue in registers
+constexpr unsigned kTsABytes = kTsM * kTsKT * 2;  // one A slice of a step
+
+template <int NN>
+__global__ void __launch_bounds__(kTsThreads, 1)
+    tsm_q_tc5_kernel(int64_t n, float *Qout, int64_t ldo, const float *__restrict__ Qin,
+                     int64_t ldq, const float *S, int64_t lds, const double *__restrict__ beta,
+                     int tmem_half, int *__restrict__ status) {
+    constexpr int K = 16 * NN;               // = k = N
+    constexpr int Kp = (K + 31) / 32 * 32;   // K padded to whole steps
+    constexpr int KS = Kp / kTsKT;           // steps per tile
+    constexpr unsigned w_bytes = K * Kp * 2;  // one slice of beta^T (N x Kp)
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // [beta slices 3 x w_bytes][A slices 2 x 3 x kTsABytes][ring][mbar x6][tmem slot][abort]
+    unsigned char *wsl = smem_raw;
+    unsigned char *asl = smem_raw + 3 * w_bytes;
+    float *ring = reinterpret_cast<float *>(asl + 2 * 3 * kTsABytes);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(ring + kTsStages * kTsM * kTsRingLd);
+    uint64_t *mma_done = mbar, *acc_full = mbar + 2, *acc_empty = mbar + 4;
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(mbar + 6);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t ntiles = (n + kTsM - 1) / kTsM;
+    const int64_t my_tiles =
+        ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t nsteps = my_tiles * KS;
+
+    // ---- setup: beta^T slices (B operand: row c = output column, K-major),
+    // zero-padded to Kp; barriers; TMEM (two accumulator buffers)
+    for (int pidx = tid; pidx < K * Kp / 2; pidx += kTsThreads) {
+        const int c = pidx / (Kp / 2), j = 2 * (pidx % (Kp / 2));
+        const float w0 = j < K ? (float)beta[(size_t)j * K + c] : 0.f;
+        const float w1 = j + 1 < K ? (float)beta[(size_t)(j + 1) * K + c] : 0.f;
+        unsigned hw, mw, lw;
+        t5_split2(w0, w1, hw, mw, lw);
+        const unsigned off = (((c >> 3) * (Kp / 8) + (j >> 3)) * 64 + (c & 7) * 8 + (j & 7)) * 2;
+        *reinterpret_cast<unsigned *>(wsl + off) = hw;
+        *reinterpret_cast<unsigned *>(wsl + w_bytes + off) = mw;
+        *reinterpret_cast<unsigned *>(wsl + 2 * w_bytes + off) = lw;
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            t5_mbar_init(&mma_done[i], 1);
+            t5_mbar_init(&acc_full[i], 1);
+            t5_mbar_init(&acc_empty[i], kTsEpi / 32);
+        }
+        *abort_flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         t5_smem_u32(tmem_slot)),
+                     "r"(2 * tmem_half));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    t5_fence_proxy_async();
+    t5_fence_before();
+    __syncthreads();
+    t5_fence_after();
+    const unsigned tmem = *tmem_slot;
+
+    if (warp < kTsProd / 32) {
+        // ================================ producers
+        auto tile_row0 = [&](int64_t tj) { return (blockIdx.x + tj * gridDim.x) * (int64_t)kTsM; };
+        auto issue_loads = [&](int64_t j) {
+            if (j < nsteps) {
+                float *dst = ring + (int)(j % kTsStages) * kTsM * kTsRingLd;
+                const int64_t r0 = tile_row0(j / KS);
+                const int c0 = (int)(j % KS) * kTsKT;
+#pragma unroll
+                for (int v = 0; v < kTsM * kTsKT / 4 / kTsProd; ++v) {
+                    const int id = tid + v * kTsProd;
+                    const int r = id >> 3, c4 = id & 7;
+                    const int64_t row = r0 + r;
+                    const int col = c0 + 4 * c4;
+                    const bool ok = row < n && col < K;
+                    t5_cp16(dst + r * kTsRingLd + 4 * c4, ok ? (const void *)(Qin + row * ldq + col) : Qin,
+                            ok ? 16 : 0);
+                }
+            }
+            t5_cp_commit();
+        };
+        auto convert = [&](int stage, int buf) {
+            const float *src = ring + stage * kTsM * kTsRingLd;
+            unsigned char *dst = asl + buf * 3 * kTsABytes;
+#pragma unroll
+            for (int u = 0; u < kTsM * kTsKT / 8 / kTsProd; ++u) {
+                const int id = tid + u * kTsProd;
+                const int q = id & 7, o = (id >> 3) & 3, g = id >> 5;
+                const int row = 8 * g + q;
+                const float4 x0 = *reinterpret_cast<const float4 *>(src + row * kTsRingLd + 8 * o);
+                const float4 x1 =
+                    *reinterpret_cast<const float4 *>(src + row * kTsRingLd + 8 * o + 4);
+                unsigned hw[4], mw[4], lw[4];
+                t5_split2(x0.x, x0.y, hw[0], mw[0], lw[0]);
+                t5_split2(x0.z, x0.w, hw[1], mw[1], lw[1]);
+                t5_split2(x1.x, x1.y, hw[2], mw[2], lw[2]);
+                t5_split2(x1.z, x1.w, hw[3], mw[3], lw[3]);
+                const unsigned off = ((row >> 3) * (kTsKT / 8) + o) * 128 + (row & 7) * 16;
+                *reinterpret_cast<uint4 *>(dst + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(dst + kTsABytes + off) =
+                    make_uint4(mw[0], mw[1], mw[2], mw[3]);
+                *reinterpret_cast<uint4 *>(dst + 2 * kTsABytes + off) =
+                    make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+        };
+        constexpr unsigned idesc = t5_idesc(kTsM, K);
+        // thread 0: the 12 MMAs of step j; false if the accumulator buffer
+        // did not come free in time
+        auto issue_mma = [&](int64_t j) -> bool {
+            const int buf = (int)(j & 1);
+            const int64_t tj = j / KS;
+            const int kc = (int)(j % KS);
+            const int tb = (int)(tj & 1);
+            if (kc == 0 && tj >= 2) {
+                if (!t5_mbar_wait(&acc_empty[tb], (unsigned)(((tj - 2) >> 1) & 1))) return false;
+                t5_fence_after();
+            }
+            const unsigned d = tmem + (unsigned)(tb * tmem_half);
+            const unsigned abase = t5_smem_u32(asl + buf * 3 * kTsABytes);
+            const unsigned wbase = t5_smem_u32(wsl);
+            unsigned accumulate = kc != 0;
+            const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+            for (int pr = 0; pr < 6; ++pr) {
+#pragma unroll
+                for (int kk = 0; kk < kTsKT / 16; ++kk) {
+                    if (kc * kTsKT + kk * 16 >= K) continue;  // K-padding half
+                    const uint64_t ad = t5_desc(abase + pa[pr] * kTsABytes + kk * 256, 512);
+                    const uint64_t bd = t5_desc(wbase + pb[pr] * w_bytes + (kc * 4 + kk * 2) * 128,
+                                                (Kp / 8) * 128);
+                    t5_mma(d, ad, bd, idesc, accumulate);
+                    accumulate = 1;
+                }
+            }
+            t5_commit(&mma_done[buf]);
+            if (kc == KS - 1) t5_commit(&acc_full[tb]);
+            return true;
+        };
+
+        int timed_out = 0, aborted = 0;
+        int64_t last_committed = -1;
+        for (int j = 0; j < kTsStages - 1; ++j) issue_loads(j);
+        for (int64_t i = 0; i <= nsteps; ++i) {
+            if (i < nsteps) asm volatile("cp.async.wait_group %0;\n" ::"n"(kTsStages - 2));
+            t5_fence_proxy_async();
+            t5_fence_before();
+            aborted = t5_bar_or(1, kTsProd, timed_out);
+            t5_fence_after();
+            if (aborted) break;
+            if (i >= 1 && tid == 0) {
+                if (issue_mma(i - 1)) {
+                    last_committed = i - 1;
+                } else {
+                    atomicOr(status, kStatusTimeout);
+                    timed_out = 1;
+                }
+            }
+            if (i == nsteps) break;
+            issue_loads(i + kTsStages - 1);
+            if (i >= 2 && !__all_sync(0xffffffffu, t5_mbar_wait(&mma_done[i & 1],
+                                                                (unsigned)(((i - 2) >> 1) & 1)))) {
+                if (lane == 0) atomicOr(status, kStatusTimeout);
+                timed_out = 1;
+            }
+            convert((int)(i % kTsStages), (int)(i & 1));
+        }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        if (aborted) {
+            if (tid == 0) {
+                *abort_flag = 1;
+                if (last_committed >= 0)
+                    t5_mbar_wait(&mma_done[last_committed & 1],
+                                 (unsigned)((last_committed >> 1) & 1));
+            }
+        }
+    } else {
+        // ================================ epilogue: rows 32 * quad + lane of each tile
+        const int quad = warp & 3;
+        for (int64_t tj = 0; tj < my_tiles; ++tj) {
+            const int64_t row = (blockIdx.x + tj * gridDim.x) * (int64_t)kTsM + 32 * quad + lane;
+            const bool rv = row < n;
+            float4 sv[NN * 4];
+#pragma unroll
+            for (int q = 0; q < NN * 4; ++q)
+                sv[q] = rv ? *reinterpret_cast<const float4 *>(S + row * lds + 4 * q)
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+            const int tb = (int)(tj & 1);
+            const bool ok = __all_sync(0xffffffffu, t5_mbar_wait_or_abort(
+                                                        &acc_full[tb], (unsigned)((tj >> 1) & 1),
+                                                        abort_flag));
+            if (!ok) {
+                if (lane == 0) {
+                    if (!*abort_flag) atomicOr(status, kStatusTimeout);
+                    *abort_flag = 1;
+                }
+                break;
+            }
+            t5_fence_after();
+            const unsigned tbase = tmem + ((unsigned)(32 * quad) << 16) + (unsigned)(tb * tmem_half);
+#pragma unroll
+            for (int c8 = 0; c8 < 2 * NN; ++c8) {
+                float v[8];
+                t5_ld8(tbase + 8 * c8, v);
+                const float4 a = sv[2 * c8], b = sv[2 * c8 + 1];
+                if (rv) {
+                    float4 *o = reinterpret_cast<float4 *>(Qout + row * ldo + 8 * c8);
+                    o[0] = make_float4(a.x - v[0], a.y - v[1], a.z - v[2], a.w - v[3]);
+                    o[1] = make_float4(b.x - v[4], b.y - v[5], b.z - v[6], b.w - v[7]);
+                }
+            }
+            t5_fence_before();
+            __syncwarp();
+            if (lane == 0) t5_mbar_arrive(&acc_empty[tb]);
+        }
+    }
+    t5_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        t5_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                     "r"(2 * tmem_half));
+    }
+}
+
+static size_t tsm_q_smem(int k) {
+    const int Kp = (k + 31) / 32 * 32;
+    return 3 * (size_t)k * Kp * 2 + 2 * 3 * (size_t)kTsABytes +
+           (size_t)kTsStages * kTsM * kTsRingLd * 4 + 6 * 8 + 16;
+}
+
+bool tsm_q_tc5_supported(int k) {
+    return k >= 16 && k % 16 == 0 && k / 16 <= kTsMaxNN && tsm_q_smem(k) <= max_smem_optin();
+}
+
+template <int NN>
+static int launch_tsm_q(cudaStream_t st, int64_t n, float *Qout, int64_t ldo, const float *Qin,
+                        int64_t ldq, const float *S, int64_t lds, const double *beta,
+                        int *status) {
+    const int k = 16 * NN;
+    const size_t smem = tsm_q_smem(k);
+    static const bool attr = [] {
+        cudaFuncSetAttribute(tsm_q_tc5_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    int tmem_half = 32;
+    while (tmem_half < k) tmem_half *= 2;
+    const int64_t ntiles = (n + kTsM - 1) / kTsM;
+    const int grid = (int)std::min<int64_t>(ntiles, sm_count());
+    tsm_q_tc5_kernel<NN><<<grid, kTsThreads, smem, st>>>(n, Qout, ldo, Qin, ldq, S, lds, beta,
+                                                         tmem_half, status);
+    return check_launch();
+}
+
+int launch_qupdate_tc5(cudaStream_t st, int64_t n, int k, float *Qout, int64_t ldo,
+                       const float *Qin, int64_t ldq, const float *S, int64_t lds,
+                       const double *beta, int *status) {
+    if (n < 0 || !beta || !status) return CACG_ERR_ARG;
+    if (!tsm_q_tc5_supported(k) || ldq % 4 || ldo % 4 || lds % 4 || !aligned16(Qin) ||
+        !aligned16(Qout) || !aligned16(S))
+        return CACG_ERR_UNSUPPORTED;
+    if (n == 0) return CACG_OK;
+    switch (k / 16) {
+        case 1: return launch_tsm_q<1>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status);
+        case 2: return launch_tsm_q<2>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status);
+        case 3: return launch_tsm_q<3>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status);
+        case 4: return launch_tsm_q<4>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status);
+        case 5: return launch_tsm_q<5>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status);
+        case 6: return launch_tsm_q<6>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status);
+    }
+    return CACG_ERR_UNSUPPORTED;
+}
+
+}  // namespace cacg

@@ -929,14 +929,31 @@ extern "C" int cacg_k_qupdate(int32_t vtype, int64_t n, int32_t k, void *Q, int6
     if (cudaMallocAsync(&Qin, bytes > 0 ? bytes : 16, st) != cudaSuccess) return CACG_ERR_OOM;
     cudaMemcpyAsync(Qin, Q, bytes, cudaMemcpyDeviceToDevice, st);
     int rc;
-    if (vtype == CACG_VAL_F64)
+    if (vtype == CACG_VAL_F64) {
         rc = launch_qupdate<double>(st, n, k, (double *)Q, ldq, (const double *)Qin, ldq,
                                     (const double *)S, lds, beta);
-    else if (vtype == CACG_VAL_F32)
+    } else if (vtype == CACG_VAL_F32) {
         rc = launch_qupdate<float>(st, n, k, (float *)Q, ldq, (const float *)Qin, ldq,
                                    (const float *)S, lds, beta);
-    else
+    } else if (vtype == (CACG_VAL_F32 | CACG_VAL_TC5)) {
+        int *dstat = nullptr;
+        if (cudaMallocAsync((void **)&dstat, sizeof(int), st) != cudaSuccess) {
+            cudaFreeAsync(Qin, st);
+            return CACG_ERR_OOM;
+        }
+        cudaMemsetAsync(dstat, 0, sizeof(int), st);
+        rc = launch_qupdate_tc5(st, n, k, (float *)Q, ldq, (const float *)Qin, ldq,
+                                (const float *)S, lds, beta, dstat);
+        int hstat = 0;
+        if (rc == CACG_OK) {
+            cudaMemcpyAsync(&hstat, dstat, sizeof(int), cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) rc = CACG_ERR_CUDA;
+            else if (hstat & kStatusTimeout) rc = CACG_ERR_TIMEOUT;
+        }
+        cudaFreeAsync(dstat, st);
+    } else {
         rc = CACG_ERR_ARG;
+    }
     cudaFreeAsync(Qin, st);
     return rc;
 }

@@ -608,12 +608,18 @@ struct Solver {
             // Q_new = S - Q_old beta, written over S; then S <-> Q
             prof.begin(CACG_PHASE_QUPDATE, 3.0 * dn * k * ees, 2.0 * dn * k * k);
             if constexpr (std::is_same<T, float>::value) {
-                if (slices)
+                if (slices) {
                     rc = launch_qupdate_sl(st, n, k, (float *)b.S, k, (const float *)b.Q, k,
                                            (const float *)b.S, k, b.beta, b.Ssl);
-                else
-                    rc = launch_qupdate<T>(st, n, k, (T *)b.S, k, (const T *)b.Q, k,
-                                           (const T *)b.S, k, b.beta);
+                } else {
+                    rc = CACG_ERR_UNSUPPORTED;
+                    if (tensor_cores5())
+                        rc = launch_qupdate_tc5(st, n, k, (float *)b.S, k, (const float *)b.Q, k,
+                                                (const float *)b.S, k, b.beta, b.status);
+                    if (rc == CACG_ERR_UNSUPPORTED)
+                        rc = launch_qupdate<T>(st, n, k, (T *)b.S, k, (const T *)b.Q, k,
+                                               (const T *)b.S, k, b.beta);
+                }
             } else {
                 rc = launch_qupdate<T>(st, n, k, (T *)b.S, k, (const T *)b.Q, k, (const T *)b.S,
                                        k, b.beta);
@@ -659,6 +665,12 @@ struct Solver {
     }
 
     double sa = 0, sb = 0;
+
+    // mixed mode on the tcgen05 kernels (Gram, Q update) unless a CUDA-core
+    // or mma.sync Gram variant is requested
+    bool tensor_cores5() const {
+        return p.gram_variant == CACG_GRAM_AUTO || p.gram_variant == CACG_GRAM_TC5;
+    }
 
     // Gram with the variant for this precision: the mixed mode uses the
     // tensor-core kernel unless a CUDA-core variant is requested.

@@ -63,11 +63,17 @@ extern "C" {
 #define CACG_GRAM_TC_SLICES 4 /* same products, from bf16 slice planes written by the
                                  producers (cacg_k_gram splits its inputs first) */
 #define CACG_GRAM_TC5 5  /* same products on the 5th-generation tensor cores
-                            (tcgen05.mma, accumulator in tensor memory) */
+                            (tcgen05.mma, accumulator in tensor memory, float-float
+                            sums across 256-row groups) */
 
 #define CACG_VAL_F64 0
 #define CACG_VAL_F32 1
 #define CACG_XR_EXACT 16 /* or-ed into cacg_k_xrupdate's vtype: float-float sums */
+#define CACG_VAL_TC5 32  /* or-ed into cacg_k_qupdate's vtype (FP32 only): the product
+                            on the 5th-generation tensor cores (three bf16 slices per
+                            value, six slice products, FP32 accumulation); returns
+                            CACG_ERR_UNSUPPORTED unless k is a multiple of 16, k <= 96,
+                            and the rows are 16-byte aligned */
 
 /* generators (cacg_gen_*) */
 #define CACG_GEN_LAPLACE2D_5PT 1

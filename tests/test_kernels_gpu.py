@@ -63,6 +63,58 @@ def test_spmm_f32(lib, torch_cuda, w):
     assert relerr(host(Y), want) <= 2e-6
 
 
+def _irregular_csr(n, seed):
+    """Random CSR with empty rows, short rows and a few rows of ~600 entries
+    (a warp block of such rows exceeds the staged-entry capacity)."""
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(0, 12, n)
+    lens[rng.choice(n, 5, replace=False)] = 600
+    lens[rng.choice(n, 7, replace=False)] = 0
+    rp = np.zeros(n + 1, np.int32)
+    rp[1:] = np.cumsum(lens)
+    ci = np.concatenate([np.sort(rng.choice(n, int(L), replace=False)) for L in lens]).astype(np.int32)
+    v = rng.standard_normal(int(rp[-1]))
+    return rp, ci, v
+
+
+@pytest.mark.parametrize("w", [2, 16, 96])
+@pytest.mark.parametrize("f32", [False, True])
+def test_spmm_irregular_rows(lib, torch_cuda, w, f32):
+    torch = torch_cuda
+    n = 5003
+    rp, ci, v = _irregular_csr(n, 21)
+    dt = np.float32 if f32 else np.float64
+    X = O.gen_rhs("normal", n, w, 22).astype(dt)
+    Z1 = O.gen_rhs("normal", n, w, 23).astype(dt)
+    vv = v.astype(dt)
+    want = 0.5 * O.port_spmm(rp, ci, vv.astype(np.float64), X.astype(np.float64)) \
+        - 2.0 * Z1.astype(np.float64)
+    d = {k: dev(torch, a) for k, a in dict(rp=rp, ci=ci, v=vv, X=X, Z1=Z1).items()}
+    Y = torch.empty((n, w), dtype=torch.float32 if f32 else torch.float64, device="cuda")
+    rc = lib.cacg_k_spmm(F32 if f32 else F64, n, ptr(d["rp"]), ptr(d["ci"]), ptr(d["v"]), w,
+                         ptr(d["X"]), w, ptr(Y), w, ptr(d["Z1"]), w, None, 0, 0.5, -2.0, 0.0, None)
+    assert rc == 0
+    assert relerr(host(Y), want) <= (5e-6 if f32 else 1e-13)
+
+
+@pytest.mark.parametrize("w", [3, 16])
+def test_spmm_unaligned_index_arrays(lib, torch_cuda, w):
+    """ci / val starting off a 16-byte boundary take the unstaged path."""
+    torch = torch_cuda
+    rp, ci, v = _mat("st3d27", 9)
+    n = len(rp) - 1
+    X = O.gen_rhs("normal", n, w, 24)
+    want = O.port_spmm(rp, ci, v, X)
+    ci_pad = np.concatenate([np.zeros(1, np.int32), ci])
+    v_pad = np.concatenate([np.zeros(1), v])
+    d = {k: dev(torch, a) for k, a in dict(rp=rp, ci=ci_pad, v=v_pad, X=X).items()}
+    Y = torch.empty((n, w), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_spmm(F64, n, ptr(d["rp"]), ptr(d["ci"]) + 4, ptr(d["v"]) + 8, w, ptr(d["X"]),
+                         w, ptr(Y), w, None, 0, None, 0, 1.0, 0.0, 0.0, None)
+    assert rc == 0
+    assert relerr(host(Y), want) <= 1e-13
+
+
 @pytest.mark.parametrize("kind,N,m,s", [("lap2d", 48, 1, 4), ("lap3d7", 12, 8, 8),
                                         ("st3d27", 10, 16, 6), ("lap3d7", 10, 3, 5)])
 def test_basis_matches_reference(lib, torch_cuda, kind, N, m, s):
@@ -138,6 +190,38 @@ def test_qupdate(lib, torch_cuda, vt, n, k):
     rc = lib.cacg_k_qupdate(vt, n, k, ptr(dq), k, ptr(ds), k, ptr(db), None)
     assert rc == 0
     assert relerr(host(dq), want) <= (1e-13 if vt == F64 else 3e-6)
+
+
+TC5 = 32
+
+
+@pytest.mark.parametrize("n,k", [(10000, 64), (30000, 96), (999, 16), (4099, 48), (127, 32),
+                                 (200001, 96)])
+def test_qupdate_tcgen05(lib, torch_cuda, n, k):
+    """Q = S - Q beta on the tcgen05 tensor cores (bf16x3 slices, six products,
+    FP32 accumulation): within 3e-6 of the FP64 product of the FP32 inputs,
+    like the CUDA-core FP32 kernel."""
+    torch = torch_cuda
+    Qh = O.gen_rhs("normal", n, k, 1).astype(np.float32)
+    Sh = O.gen_rhs("normal", n, k, 2).astype(np.float32)
+    beta = O.gen_rhs("normal", k, k, 3)
+    bh = beta.astype(np.float32).astype(np.float64)
+    want = Sh.astype(np.float64) - O.port_tallsmall(Qh.astype(np.float64), bh)
+    dq, ds, db = dev(torch, Qh), dev(torch, Sh), dev(torch, beta)
+    rc = lib.cacg_k_qupdate(F32 | TC5, n, k, ptr(dq), k, ptr(ds), k, ptr(db), None)
+    assert rc == 0
+    assert relerr(host(dq), want) <= 3e-6
+
+
+@pytest.mark.parametrize("k", [12, 112, 128])
+def test_qupdate_tcgen05_rejects_unsupported_widths(lib, torch_cuda, k):
+    torch = torch_cuda
+    n = 100
+    dq = torch.zeros((n, k), dtype=torch.float32, device="cuda")
+    ds = torch.zeros((n, k), dtype=torch.float32, device="cuda")
+    db = torch.zeros((k, k), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_qupdate(F32 | TC5, n, k, ptr(dq), k, ptr(ds), k, ptr(db), None)
+    assert rc == -6
 
 
 @pytest.mark.parametrize("vt,exact", [(F64, False), (F64, True), (F32, False), (F32, True)])
@@ -219,7 +303,8 @@ def test_gerschgorin_exact(lib, torch_cuda, kind, N):
 @pytest.mark.parametrize("variant", [3, 4, 5])
 @pytest.mark.parametrize("n,ka,kb1,kb2", [(100000, 96, 96, 16), (200000, 96, 96, 0),
                                           (5000, 24, 24, 4), (40000, 64, 64, 8),
-                                          (30000, 128, 128, 32), (3001, 12, 12, 3), (33, 4, 4, 1)])
+                                          (30000, 128, 128, 32), (3001, 12, 12, 3), (33, 4, 4, 1),
+                                          (20000, 160, 160, 16)])
 def test_gram_tensor_core_bf16_slices(lib, torch_cuda, variant, n, ka, kb1, kb2):
     """FP32 inputs on the bf16 tensor cores (three slices, six products,
     FP32 over 256-row groups, FP64 across): normwise within 4e-6 of the exact
@@ -236,5 +321,24 @@ def test_gram_tensor_core_bf16_slices(lib, torch_cuda, variant, n, ka, kb1, kb2)
     rc = lib.cacg_k_gram(F32, variant, n, ptr(d["L"]), ka, ka, ptr(d["R1"]), kb1, kb1,
                          ptr(d["R2"]) if kb2 else None, kb2 if kb2 else 8, kb2, ptr(C), kb1 + kb2,
                          None)
+    assert rc == 0
+    assert relerr(host(C), want) <= 4e-6
+
+
+@pytest.mark.parametrize("n", [7, 4099, 70001])
+def test_gram_tc5_padded_rows_partial_chunks(lib, torch_cuda, n):
+    """tcgen05 Gram on sub-blocks of wider arrays: L = 6 of 8 columns,
+    R1 = 4 of 8, R2 = 3 of 4 (16-byte row copies that end inside a chunk are
+    zero-filled past the block's last column)."""
+    torch = torch_cuda
+    Lw = O.gen_rhs("normal", n, 8, 11).astype(np.float32)
+    R1w = O.gen_rhs("normal", n, 8, 12).astype(np.float32)
+    R2w = O.gen_rhs("normal", n, 4, 13).astype(np.float32)
+    want = O.port_gram(Lw[:, :6].astype(np.float64),
+                       np.hstack([R1w[:, :4], R2w[:, :3]]).astype(np.float64))
+    d = {k_: dev(torch, a) for k_, a in dict(L=Lw, R1=R1w, R2=R2w).items()}
+    C = torch.zeros((6, 7), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_gram(F32, 5, n, ptr(d["L"]), 8, 6, ptr(d["R1"]), 8, 4, ptr(d["R2"]), 4, 3,
+                         ptr(C), 7, None)
     assert rc == 0
     assert relerr(host(C), want) <= 4e-6
