@@ -360,6 +360,41 @@ def run_gpu_arm(args, w, rank, world):
     return out, info64["iterations"]
 
 
+SERVING = dict(s=4, tol=1e-8, maxit=3000, rr=5, max_active=4, budget_gb=120, seed=4,
+               calib=32)
+
+
+def run_serving(args):
+    """Serving stream (Poisson arrivals of 2-D 5-point / 3-D 7-point
+    Laplacians, n log-uniform in [1e3, 1e6], shift U[0, 0.1], 1-16 N(0,1)
+    RHS, seed 4) through the continuous-batching server, FP64 and mixed.
+    Load = arrival rate / closed-burst capacity measured on the first
+    `calib` requests of the same stream."""
+    import cacg_gb300 as cg
+    from cacg_gb300 import serving as SV
+
+    K = args.serving_requests
+    specs = SV.request_specs(K, seed=SERVING["seed"])
+    calib = specs[:min(SERVING["calib"], K)]
+    budget = SERVING["budget_gb"] << 30
+    out = {"workload": "2-D 5-pt / 3-D 7-pt Laplacians 50/50, n log-uniform [1e3, 1e6], "
+                       "shift U[0, 0.1], 1-16 N(0,1) RHS, seed 4, Poisson arrivals",
+           "requests": K, "load": args.serving_load, "max_active": SERVING["max_active"],
+           "mem_budget_gb": SERVING["budget_gb"], "s": SERVING["s"], "tol": SERVING["tol"],
+           "latency": "completion - scheduled arrival (queueing, admission, copies, solve)"}
+    for prec in ("mixed", "fp64"):
+        p = cg.Params(s=SERVING["s"], bounds="gerschgorin", tol=SERVING["tol"],
+                      maxit=SERVING["maxit"], precision=prec, rr_period=SERVING["rr"])
+        cal = SV.run(calib, p, None, budget, SERVING["max_active"])
+        rate = args.serving_load * cal["requests_per_s"]
+        res = SV.run(specs, p, rate, budget, SERVING["max_active"])
+        summ = SV.summarize(res, specs, SERVING["tol"])
+        summ["capacity_requests_per_s"] = cal["requests_per_s"]
+        summ["arrival_rate_per_s"] = rate
+        out[prec] = summ
+    return out
+
+
 def traffic_for(phase):
     p = os.path.join(HERE, "profiles", "traffic.json")
     try:
@@ -392,6 +427,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="st27_128_m16", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serving-requests", type=int, default=300,
+                    help="requests of the serving stream per precision (0: skip)")
+    ap.add_argument("--serving-load", type=float, default=0.7)
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -404,6 +442,11 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
     out, it64 = run_gpu_arm(args, w, rank, world)
+    if rank == 0 and args.serving_requests > 0:
+        srv = run_serving(args)
+        out["serving"] = srv
+        out["p50_latency_ms"] = srv["mixed"]["p50_ms"]
+        out["p99_latency_ms"] = srv["mixed"]["p99_ms"]
     if rank == 0:
         if not args.no_cpu_baseline:
             cb = reference_sample(args.workload, w, it64, os.cpu_count() or 1)

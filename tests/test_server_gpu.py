@@ -70,3 +70,19 @@ def test_oversized_request_refused(lib):
         srv.submit(rp, ci, v, B, cg.Params())
     srv.close()
     assert e.value.code == -7
+
+
+def test_open_loop_driver_small_stream(lib):
+    """The load driver: Poisson arrivals of small serving-workload requests,
+    every request converges and gets a latency >= its own solve time."""
+    from cacg_gb300 import serving as SV
+
+    specs = SV.request_specs(16, seed=7, nmin=1e3, nmax=2e4)
+    p = cg.Params(s=4, bounds="gerschgorin", tol=1e-8, maxit=3000, precision="mixed")
+    res = SV.run(specs, p, rate=200.0, mem_budget=4 << 30, max_active=4)
+    summ = SV.summarize(res, specs, 1e-8)
+    assert summ["all_converged"], summ
+    assert len(res["latency_s"]) == 16
+    for lat, info in zip(res["latency_s"], res["infos"]):
+        assert lat >= info["seconds"] * 0.99
+    assert summ["p99_ms"] >= summ["p50_ms"] > 0
