@@ -19,6 +19,7 @@ BOUNDS_GERSCHGORIN, BOUNDS_GIVEN, BOUNDS_LANCZOS = 0, 1, 2
 TOL_ABS_COL0, TOL_REL_ALL = 0, 1
 FP64, MIXED = 0, 1
 GRAM_AUTO, GRAM_FMA, GRAM_DMMA, GRAM_TC, GRAM_TC_SLICES, GRAM_TC5 = 0, 1, 2, 3, 4, 5
+SPMM_AUTO, SPMM_CSR = 0, 1
 VAL_F64, VAL_F32 = 0, 1
 
 
@@ -34,7 +35,8 @@ class CacgParams(C.Structure):
                 ("precision", C.c_int32), ("rr_period", C.c_int32),
                 ("gram_variant", C.c_int32), ("lanczos_seed", C.c_uint64),
                 ("stream", C.c_void_p), ("use_graph", C.c_int32),
-                ("exact_updates", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("exact_updates", C.c_int32), ("spmm_format", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class CacgResult(C.Structure):
@@ -82,6 +84,7 @@ _SIGS = {
     "cacg_matrix_create": (C.c_int, [C.POINTER(CacgCsr), C.c_int32, C.POINTER(C.c_void_p)]),
     "cacg_matrix_destroy": (C.c_int, [C.c_void_p]),
     "cacg_matrix_device_bytes": (C.c_int64, [C.c_void_p]),
+    "cacg_matrix_diagonals": (C.c_int32, [C.c_void_p]),
     "cacg_solve_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                     C.POINTER(CacgParams), C.POINTER(CacgResult)]),
     "cacg_workspace_bytes": (C.c_int64, [C.c_int64, C.c_int32, C.c_int32, C.c_int32]),

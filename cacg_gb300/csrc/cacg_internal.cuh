@@ -65,6 +65,15 @@ __device__ __forceinline__ void vload(float (&d)[4], const float *p) {
     float4 v = __ldg(reinterpret_cast<const float4 *>(p));
     d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
 }
+// generic-pointer vector loads (shared or global memory)
+__device__ __forceinline__ void vload_plain(double (&d)[2], const double *p) {
+    double2 v = *reinterpret_cast<const double2 *>(p);
+    d[0] = v.x; d[1] = v.y;
+}
+__device__ __forceinline__ void vload_plain(float (&d)[4], const float *p) {
+    float4 v = *reinterpret_cast<const float4 *>(p);
+    d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+}
 __device__ __forceinline__ void vstore(double *p, const double (&d)[2]) {
     *reinterpret_cast<double2 *>(p) = make_double2(d[0], d[1]);
 }
@@ -142,6 +151,9 @@ int launch_residual(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t
                     const double *val, int m, const double *X, const double *B,
                     double *R, void *S0, int s0_is_f32, int64_t lds, double *norms,
                     double *ws, double avg_nnz);
+// Second half of launch_residual, for an R = B - A X formed elsewhere.
+int launch_residual_post(cudaStream_t st, int64_t n, int m, double *R, void *S0, int s0_is_f32,
+                         int64_t lds, double *norms, double *ws);
 // Residual for the mixed mode: also R32 = (float)R and the slice planes of S0, R32.
 int launch_residual_sl(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
                        const double *val, int m, const double *X, const double *B, double *R,

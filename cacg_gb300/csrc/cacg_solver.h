@@ -9,20 +9,46 @@
 
 namespace cacg {
 
+constexpr int kDiaMax = 32;      // diagonals of a DIA view
+constexpr int kDiaGroupMax = 4;  // adjacent diagonals sharing one X register window
+
+// Diagonal offsets (sorted) and groups of adjacent offsets of a DIA view;
+// passed to kernels by value.
+struct DiaDesc {
+    int ndiag, ngroups;
+    int64_t off[kDiaMax];
+    int gstart[kDiaMax + 1];
+};
+
 // A CSR matrix resident on the device: int32 indices, FP64 values, and FP32
-// values when the mixed mode needs them.
+// values when the mixed mode needs them; plus a DIA view (values per
+// diagonal, ndiag x dia_npad, zero where a row lacks the diagonal) when every
+// nonzero lies on one of at most kDiaMax diagonals with little padding.
 struct DevMatrix {
     int64_t n = 0, nnz = 0;
     double avg_nnz = 0;
     int32_t *rp = nullptr, *ci = nullptr;
     double *val = nullptr;
     float *val32 = nullptr;
+    int dia_ndiag = 0;  // 0: CSR only
+    int64_t dia_npad = 0;
+    DiaDesc dia{};
+    double *dia64 = nullptr;
+    float *dia32 = nullptr;
     size_t owned_bytes = 0;
     cudaStream_t st = nullptr;  // stream of the stream-ordered allocations
     static int create(const cacg_csr *A, bool want_f32, DevMatrix *M, cudaStream_t st);
+    int build_dia(const cacg_csr *A, bool want_f32, cudaStream_t st);
     int ensure_f32(cudaStream_t st);
     void release();
 };
+
+// Y = ca A X + cb Z1 + cc Z2 over the DIA view (k_dia.cu);
+// CACG_ERR_UNSUPPORTED when the matrix has no view of this precision.
+template <typename T>
+int launch_dia_spmm(cudaStream_t st, const DevMatrix *A, int w, const T *X, int64_t ldx, T *Y,
+                    int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2, int64_t ldz2,
+                    double ca, double cb, double cc);
 
 // Device bytes of one solve's state (S, Q, AQ, R, small matrices, reduction
 // workspaces), the admission cost of a request.

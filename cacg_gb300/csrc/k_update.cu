@@ -686,6 +686,13 @@ int launch_residual(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t
     int rc = launch_spmm<double>(st, n, rp, ci, val, m, X, m, R, m, B, m, nullptr, 0, -1.0,
                                  1.0, 0.0, avg_nnz);
     if (rc != CACG_OK) return rc;
+    return launch_residual_post(st, n, m, R, S0, s0_is_f32, lds, norms, ws);
+}
+
+// R = B - A X already formed: S0 = cast(R), norm partials, column norms.
+int launch_residual_post(cudaStream_t st, int64_t n, int m, double *R, void *S0, int s0_is_f32,
+                         int64_t lds, double *norms, double *ws) {
+    int rc;
     if (m > kRowThreads) return CACG_ERR_ARG;
     int mp = pow2ceil(m);
     int rows = kRowThreads / mp;

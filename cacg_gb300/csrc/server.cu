@@ -171,8 +171,11 @@ int cacg_server_submit(cacg_server *srv, const cacg_csr *A, const double *B, int
     r->B.assign(B, B + (size_t)A->n * m);
     r->p = *p;
     r->X_out = X_out;
+    // CSR (+ FP32 values) and, for diagonal-structured matrices, the DIA view
+    // (at most 1.5 x nnz entries of FP64 + FP32 values)
     size_t mat = (size_t)(A->n + 1) * 4 + (size_t)A->nnz * (4 + 8 + 16) +
-                 (p->precision == CACG_MIXED ? (size_t)A->nnz * 4 : 0);
+                 (p->precision == CACG_MIXED ? (size_t)A->nnz * 4 : 0) + (size_t)A->nnz * 18 +
+                 (size_t)(A->n + 64) * 12 * 2;
     r->cost = mat + 2 * (size_t)A->n * m * 8 +
               solve_workspace_bytes(A->n, m, p->s, p->precision,
                                     p->bounds_mode == CACG_BOUNDS_LANCZOS);

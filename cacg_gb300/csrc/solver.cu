@@ -106,14 +106,23 @@ int DevMatrix::create(const cacg_csr *A, bool want_f32, DevMatrix *M, cudaStream
         int rc = launch_cast_f64_f32(st, A->nnz, M->val, M->val32);
         if (rc) return rc;
     }
-    return CACG_OK;
+    return M->build_dia(A, want_f32, st);
 }
 
 int DevMatrix::ensure_f32(cudaStream_t st) {
-    if (val32) return CACG_OK;
-    CACG_CUDA_TRY(cudaMallocAsync((void **)&val32, (size_t)nnz * 4 + 16, st));
-    owned_bytes += (size_t)nnz * 4;
-    return launch_cast_f64_f32(st, nnz, val, val32);
+    if (!val32) {
+        CACG_CUDA_TRY(cudaMallocAsync((void **)&val32, (size_t)nnz * 4 + 16, st));
+        owned_bytes += (size_t)nnz * 4;
+        int rc = launch_cast_f64_f32(st, nnz, val, val32);
+        if (rc) return rc;
+    }
+    if (dia_ndiag > 0 && !dia32) {
+        const int64_t cnt = (int64_t)dia_ndiag * dia_npad;
+        CACG_CUDA_TRY(cudaMallocAsync((void **)&dia32, (size_t)cnt * 4, st));
+        owned_bytes += (size_t)cnt * 4;
+        return launch_cast_f64_f32(st, cnt, dia64, dia32);
+    }
+    return CACG_OK;
 }
 
 void DevMatrix::release() {
@@ -121,10 +130,15 @@ void DevMatrix::release() {
     if (ci) cudaFreeAsync(ci, st);
     if (val) cudaFreeAsync(val, st);
     if (val32) cudaFreeAsync(val32, st);
+    if (dia64) cudaFreeAsync(dia64, st);
+    if (dia32) cudaFreeAsync(dia32, st);
     rp = nullptr;
     ci = nullptr;
     val = nullptr;
     val32 = nullptr;
+    dia64 = nullptr;
+    dia32 = nullptr;
+    dia_ndiag = 0;
     owned_bytes = 0;
 }
 
@@ -457,11 +471,19 @@ struct Solver {
     const void *val_t() const { return prec == CACG_MIXED ? (const void *)A->val32 : A->val; }
     size_t es() const { return prec == CACG_MIXED ? 4 : 8; }
 
+    // Y = ca A X + cb Z1 + cc Z2 in precision T: over the DIA view when the
+    // matrix has one (bit-identical to the CSR kernel), else over CSR.
     template <typename T>
     int spmm(const T *X, int64_t ldx, T *Y, int64_t ldy, int w, const T *Z1, int64_t ldz1,
              const T *Z2, int64_t ldz2, double ca, double cb, double cc) {
-        return launch_spmm<T>(st, A->n, A->rp, A->ci, (const T *)val_t(), w, X, ldx, Y, ldy, Z1,
-                              ldz1, Z2, ldz2, ca, cb, cc, avg_nnz);
+        if (p.spmm_format != CACG_SPMM_CSR && A->dia_ndiag > 0) {
+            int rc = launch_dia_spmm<T>(st, A, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc);
+            if (rc != CACG_ERR_UNSUPPORTED) return rc;
+        }
+        const T *v = std::is_same<T, float>::value ? (const T *)(const void *)A->val32
+                                                   : (const T *)(const void *)A->val;
+        return launch_spmm<T>(st, A->n, A->rp, A->ci, v, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2,
+                              ca, cb, cc, avg_nnz);
     }
 
     int bounds(double *lmin, double *lmax) {
@@ -506,8 +528,7 @@ struct Solver {
         double beta_prev = 0.0;
         for (int j = 0; j < steps; ++j) {
             // w = A v1 - beta_prev v0
-            rc = launch_spmm<double>(st, n, A->rp, A->ci, A->val, 1, v1, 1, w, 1, v0, 1,
-                                     nullptr, 0, 1.0, -beta_prev, 0.0, avg_nnz);
+            rc = spmm<double>(v1, 1, w, 1, 1, v0, 1, nullptr, 0, 1.0, -beta_prev, 0.0);
             if (rc) return rc;
             rc = launch_dot(st, n, w, v1, b.scal, b.norm_ws);
             if (rc) return rc;
@@ -552,9 +573,10 @@ struct Solver {
             rc = launch_residual_sl(st, A->n, A->rp, A->ci, A->val, m, X, B, R, (float *)b.S, k,
                                     b.R32, norms, b.norm_ws, avg_nnz, b.Ssl, b.R32sl);
         } else {
-            rc = launch_residual(st, A->n, A->rp, A->ci, A->val, m, X, B, R,
-                                 write_s0 ? b.S : nullptr, prec == CACG_MIXED, k, norms,
-                                 b.norm_ws, avg_nnz);
+            rc = spmm<double>(X, m, R, m, m, B, m, nullptr, 0, -1.0, 1.0, 0.0);
+            if (rc == CACG_OK)
+                rc = launch_residual_post(st, A->n, m, R, write_s0 ? b.S : nullptr,
+                                          prec == CACG_MIXED, k, norms, b.norm_ws);
             if (rc == CACG_OK && write_s0 && b.R32)
                 rc = launch_cast_f64_f32(st, A->n * m, R, b.R32);
         }
@@ -578,9 +600,12 @@ struct Solver {
                        2.0 * (double)A->nnz * m + 5.0 * dn * m);
             int rc;
             if constexpr (std::is_same<T, float>::value) {
-                rc = launch_spmm_sl<float>(st, n, A->rp, A->ci, A->val32, m, Tm1, k,
-                                           S + (size_t)j * m, k, Tm1, k, Tm2, k, ca, cb, -1.0,
-                                           avg_nnz, at(b.Ssl, (int64_t)j * m));
+                if (slices)
+                    rc = launch_spmm_sl<float>(st, n, A->rp, A->ci, A->val32, m, Tm1, k,
+                                               S + (size_t)j * m, k, Tm1, k, Tm2, k, ca, cb,
+                                               -1.0, avg_nnz, at(b.Ssl, (int64_t)j * m));
+                else
+                    rc = spmm<T>(Tm1, k, S + (size_t)j * m, k, m, Tm1, k, Tm2, k, ca, cb, -1.0);
             } else {
                 rc = spmm<T>(Tm1, k, S + (size_t)j * m, k, m, Tm1, k, Tm2, k, ca, cb, -1.0);
             }
@@ -633,11 +658,15 @@ struct Solver {
         T *AQ = (T *)b.AQ;
         prof.begin(CACG_PHASE_AQ, spmm_bytes(k, 0), 2.0 * (double)A->nnz * k);
         int rc;
-        if constexpr (std::is_same<T, float>::value)
-            rc = launch_spmm_sl<float>(st, n, A->rp, A->ci, A->val32, k, Q, k, AQ, k, nullptr, 0,
-                                       nullptr, 0, 1.0, 0.0, 0.0, avg_nnz, b.AQsl);
-        else
+        if constexpr (std::is_same<T, float>::value) {
+            if (slices)
+                rc = launch_spmm_sl<float>(st, n, A->rp, A->ci, A->val32, k, Q, k, AQ, k, nullptr,
+                                           0, nullptr, 0, 1.0, 0.0, 0.0, avg_nnz, b.AQsl);
+            else
+                rc = spmm<T>(Q, k, AQ, k, k, nullptr, 0, nullptr, 0, 1.0, 0.0, 0.0);
+        } else {
             rc = spmm<T>(Q, k, AQ, k, k, nullptr, 0, nullptr, 0, 1.0, 0.0, 0.0);
+        }
         prof.end();
         if (rc) return rc;
         const T *Rp = prec == CACG_MIXED ? (const T *)(const void *)b.R32
@@ -815,8 +844,9 @@ struct Solver {
             }
         }
         // final true residual per column (FP64)
-        rc = launch_residual(st, n, A->rp, A->ci, A->val, m, X, B, b.R, nullptr, 0, k, b.tnorm,
-                             b.norm_ws, avg_nnz);
+        rc = spmm<double>(X, m, b.R, m, m, B, m, nullptr, 0, -1.0, 1.0, 0.0);
+        if (rc == CACG_OK)
+            rc = launch_residual_post(st, n, m, b.R, nullptr, 0, k, b.tnorm, b.norm_ws);
         if (rc) return rc;
         if (p.tol_mode != CACG_TOL_REL_ALL) {
             rc = launch_colnorm(st, n, m, B, b.bnorm, b.norm_ws);
@@ -1000,6 +1030,11 @@ int cacg_matrix_destroy(cacg_matrix *A) {
 
 int64_t cacg_matrix_device_bytes(const cacg_matrix *A) {
     return A ? (int64_t)reinterpret_cast<const DevMatrix *>(A)->owned_bytes : 0;
+}
+
+int32_t cacg_matrix_diagonals(const cacg_matrix *A) {
+    if (!A) return 0;
+    return reinterpret_cast<const DevMatrix *>(A)->dia_ndiag;
 }
 
 int64_t cacg_workspace_bytes(int64_t n, int32_t m, int32_t s, int32_t precision) {

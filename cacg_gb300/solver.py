@@ -63,6 +63,7 @@ class Params:
     lanczos_seed: int = 12345
     stream: int = 0
     exact_updates: bool = False     # mixed: float-float X/R update products
+    spmm_format: str = "auto"       # "auto" (DIA view when the matrix has one) | "csr"
 
     def to_c(self) -> L.CacgParams:
         p = L.CacgParams()
@@ -88,6 +89,7 @@ class Params:
         p.lanczos_seed = self.lanczos_seed
         p.stream = self.stream or None
         p.exact_updates = 1 if self.exact_updates else 0
+        p.spmm_format = {"auto": L.SPMM_AUTO, "csr": L.SPMM_CSR}[self.spmm_format]
         return p
 
 
@@ -188,6 +190,10 @@ class Matrix:
 
     def device_bytes(self) -> int:
         return L.lib().cacg_matrix_device_bytes(self.h)
+
+    def diagonals(self) -> int:
+        """Diagonals of the DIA view (0: CSR only)."""
+        return L.lib().cacg_matrix_diagonals(self.h)
 
     def solve_device(self, B_ptr: int, X_ptr: int, m: int, params: Params):
         """B_ptr / X_ptr: device addresses of n x m row-major float64 blocks."""

@@ -66,6 +66,9 @@ extern "C" {
                             (tcgen05.mma, accumulator in tensor memory, float-float
                             sums across 256-row groups) */
 
+#define CACG_SPMM_AUTO 0
+#define CACG_SPMM_CSR 1 /* always the CSR kernels */
+
 #define CACG_VAL_F64 0
 #define CACG_VAL_F32 1
 #define CACG_XR_EXACT 16 /* or-ed into cacg_k_xrupdate's vtype: float-float sums */
@@ -113,7 +116,9 @@ typedef struct cacg_params {
     int32_t use_graph;    /* capture the outer iteration in a CUDA graph */
     int32_t exact_updates; /* MIXED: X/R update products summed in float-float
                               instead of FP32 FMAs */
-    int32_t reserved[6];
+    int32_t spmm_format;  /* CACG_SPMM_*: AUTO uses the matrix's DIA view when it
+                             has one (results bit-identical to CSR) */
+    int32_t reserved[5];
 } cacg_params;
 
 typedef struct cacg_result {
@@ -165,6 +170,11 @@ typedef struct cacg_matrix cacg_matrix;
 int cacg_matrix_create(const cacg_csr *A_host, int32_t want_fp32, cacg_matrix **out);
 int cacg_matrix_destroy(cacg_matrix *A);
 int64_t cacg_matrix_device_bytes(const cacg_matrix *A);
+/* No counterpart in the reference (CSR only there).  Diagonals of the
+ * matrix's DIA view, built at creation when every nonzero lies on one of at
+ * most 32 diagonals with at most 1.5x padding (stencil matrices); 0 when the
+ * matrix is kept as CSR only. */
+int32_t cacg_matrix_diagonals(const cacg_matrix *A);
 /* Device pointers: B_dev, X_dev are n x m row-major doubles on the device. */
 int cacg_solve_device(cacg_matrix *A, const double *B_dev, double *X_dev, int32_t m,
                       const cacg_params *p, cacg_result *res);

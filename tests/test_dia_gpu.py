@@ -1,0 +1,81 @@
+"""DIA view of stencil matrices: the solver over the DIA SpMM gives results
+bit-identical to the CSR block kernels (same FMA order per row; one column
+agrees up to rounding), and matrices that are not diagonal-structured stay
+CSR-only."""
+import numpy as np
+import pytest
+import torch
+
+import cacg_gb300 as cg
+
+pytestmark = pytest.mark.gpu
+
+
+def _solve_dev(M, B, p):
+    dB = torch.from_numpy(B).cuda()
+    dX = torch.zeros_like(dB)
+    info = M.solve_device(dB.data_ptr(), dX.data_ptr(), B.shape[1], p)
+    torch.cuda.synchronize()
+    return dX.cpu().numpy(), info
+
+
+@pytest.mark.parametrize("kind,N,ndiag,m,s", [("lap2d", 40, 5, 3, 4), ("lap3d7", 14, 7, 8, 6),
+                                              ("st3d27", 12, 27, 16, 6), ("varcoef2d", 30, 5, 4, 4),
+                                              ("lap2d", 33, 5, 1, 4)])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_dia_solve_bit_identical_to_csr(lib, kind, N, ndiag, m, s, prec):
+    rp, ci, v = cg.gen_matrix(kind, N, shift=1e-3, sigma=1.0, seed=5)
+    n = len(rp) - 1
+    B = cg.gen_rhs("normal", n, m, 3)
+    M = cg.Matrix(rp, ci, v, want_fp32=True)
+    assert M.diagonals() == ndiag
+    kw = dict(s=s, bounds="gerschgorin", tol=1e-8, maxit=400, precision=prec)
+    Xd, idia = _solve_dev(M, B, cg.Params(spmm_format="auto", **kw))
+    Xc, icsr = _solve_dev(M, B, cg.Params(spmm_format="csr", **kw))
+    M.close()
+    assert idia["status"] == 0 and icsr["status"] == 0
+    if m == 1:
+        # one column: the CSR SpMV splits a row over lanes (shuffle reduction),
+        # the DIA kernel sums the row in column order -- both converge, and
+        # the solutions agree within the solution tolerance of the parity tests
+        assert abs(idia["iterations"] - icsr["iterations"]) <= 1
+        assert idia["true_relres_max"] <= 1e-8 and icsr["true_relres_max"] <= 1e-8
+        assert np.linalg.norm(Xd - Xc) <= 1e-6 * np.linalg.norm(Xc)
+    else:
+        assert idia["iterations"] == icsr["iterations"]
+        assert np.array_equal(Xd, Xc)
+
+
+def test_dia_not_built_for_irregular_matrix(lib):
+    rng = np.random.default_rng(3)
+    n = 2000
+    rows = [np.unique(np.concatenate([[i], rng.integers(0, n, 6)])) for i in range(n)]
+    rp = np.zeros(n + 1, np.int32)
+    rp[1:] = np.cumsum([len(r) for r in rows])
+    ci = np.concatenate(rows).astype(np.int32)
+    v = rng.standard_normal(len(ci))
+    M = cg.Matrix(rp, ci, v)
+    assert M.diagonals() == 0
+    M.close()
+
+
+def test_dia_not_built_for_unsorted_rows(lib):
+    rp, ci, v = cg.gen_matrix("lap2d", 20)
+    ci = ci.copy()
+    ci[rp[50]:rp[51]] = ci[rp[50]:rp[51]][::-1]  # one row's columns reversed
+    v = v.copy()
+    v[rp[50]:rp[51]] = v[rp[50]:rp[51]][::-1]
+    M = cg.Matrix(rp, ci, v)
+    assert M.diagonals() == 0
+    M.close()
+
+
+@pytest.mark.parametrize("kind,N,ndiag", [("st3d27", 96, 27), ("lap3d7", 64, 7),
+                                          ("lap2d", 512, 5)])
+def test_dia_view_found_on_large_grids(lib, kind, N, ndiag):
+    """The offset set is exact (every nonzero hashed), independent of which
+    rows are boundary rows."""
+    rp, ci, v = cg.gen_matrix(kind, N)
+    M = cg.Matrix(rp, ci, v)
+    assert M.diagonals() == ndiag
+    M.close()
