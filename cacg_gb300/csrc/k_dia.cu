@@ -213,7 +213,7 @@ __device__ __forceinline__ void dia_cp16(void *smem, const void *g, int bytes) {
 }
 
 template <typename T, int R, int CW>
-__global__ void __launch_bounds__(kDiaThreads)
+__global__ void __launch_bounds__(kDiaThreads, R <= 4 ? 3 : 2)
     dia_spmm_kernel(int64_t n, int64_t npad, DiaDesc desc, const T *__restrict__ vals, int cpr,
                     int runs_per_block, const T *__restrict__ X, int64_t ldx, T *__restrict__ Y,
                     int64_t ldy, const T *__restrict__ Z1, int64_t ldz1,
@@ -232,9 +232,16 @@ __global__ void __launch_bounds__(kDiaThreads)
         if constexpr (R > 1) {
             if (blk < nblk) {
                 T *dst = vs + (size_t)buf * nd * BR;
-                const int per = BR / VN;
-                for (int idx = threadIdx.x; idx < nd * per; idx += blockDim.x) {
-                    const int d = idx / per, q = idx % per;
+                const int per = BR / VN;  // 16-byte chunks per diagonal
+                // (d, q) walks idx = tid, tid + blockDim, ... without a division per chunk
+                const int dstep = blockDim.x / per, qstep = blockDim.x % per;
+                int d = threadIdx.x / per, q = threadIdx.x % per;
+                for (; d < nd; d += dstep, q += qstep) {
+                    if (q >= per) {
+                        q -= per;
+                        ++d;
+                        if (d >= nd) break;
+                    }
                     const int64_t e0 = blk * BR + (int64_t)q * VN;
                     const int64_t left = npad - e0;
                     const int by = left >= VN ? 16 : (left > 0 ? (int)left * (int)sizeof(T) : 0);
@@ -265,15 +272,30 @@ __global__ void __launch_bounds__(kDiaThreads)
                 const int d0 = desc.gstart[g], G = desc.gstart[g + 1] - d0;
                 const int64_t o = desc.off[d0];
                 T win[W][CW];
+                const int64_t x0 = r0 + o;
+                if (x0 >= 0 && x0 + W <= n) {
+                    // window inside the matrix: one base pointer, constant steps
+                    const T *xp = X + x0 * ldx + (int64_t)c * CW;
 #pragma unroll
-                for (int t = 0; t < W; ++t) {
-                    if (t < R + G - 1) {
-                        int64_t xr = r0 + o + t;
-                        xr = xr < 0 ? 0 : (xr >= n ? n - 1 : xr);  // value is 0 there
-                        if constexpr (CW == 1)
-                            win[t][0] = __ldg(X + xr * ldx + c);
-                        else
-                            vload(win[t], X + xr * ldx + (int64_t)c * CW);
+                    for (int t = 0; t < W; ++t) {
+                        if (t < R + G - 1) {
+                            if constexpr (CW == 1)
+                                win[t][0] = __ldg(xp + t * ldx);
+                            else
+                                vload(win[t], xp + t * ldx);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int t = 0; t < W; ++t) {
+                        if (t < R + G - 1) {
+                            int64_t xr = x0 + t;
+                            xr = xr < 0 ? 0 : (xr >= n ? n - 1 : xr);  // value is 0 there
+                            if constexpr (CW == 1)
+                                win[t][0] = __ldg(X + xr * ldx + c);
+                            else
+                                vload(win[t], X + xr * ldx + (int64_t)c * CW);
+                        }
                     }
                 }
 #pragma unroll
@@ -334,7 +356,8 @@ static int launch_dia_kernel(cudaStream_t st, const DevMatrix *A, const T *vals,
                              int64_t ldz1, const T *Z2, int64_t ldz2, T ca, T cb, T cc) {
     const int cpr = w / CW;
     if (cpr > kDiaThreads) return CACG_ERR_UNSUPPORTED;
-    const int runs_per_block = kDiaThreads / cpr;
+    // at most 512 rows per block keeps the staged values of narrow blocks small
+    const int runs_per_block = std::min(kDiaThreads / cpr, std::max(1, 512 / R));
     const int BR = runs_per_block * R;
     const size_t smem = R > 1 ? 2 * (size_t)A->dia_ndiag * BR * sizeof(T) : 0;
     if (smem > 200 * 1024) return CACG_ERR_UNSUPPORTED;
@@ -346,7 +369,7 @@ static int launch_dia_kernel(cudaStream_t st, const DevMatrix *A, const T *vals,
     (void)attr;
     const int64_t nblk = (A->n + BR - 1) / BR;
     int per_sm = 2;
-    if (smem > 0) per_sm = std::max(1, std::min(2, (int)(220 * 1024 / smem)));
+    if (smem > 0) per_sm = std::max(1, std::min(R <= 4 ? 4 : 2, (int)(220 * 1024 / smem)));
     int64_t blocks = std::min<int64_t>(nblk, (int64_t)sm_count() * (R > 1 ? per_sm : 16));
     dia_spmm_kernel<T, R, CW><<<(unsigned)blocks, kDiaThreads, smem, st>>>(
         A->n, A->dia_npad, A->dia, vals, cpr, runs_per_block, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2,
@@ -368,6 +391,12 @@ int launch_dia_spmm(cudaStream_t st, const DevMatrix *A, int w, const T *X, int6
     const bool vec = w % VN == 0 && ldx % VN == 0 && ldy % VN == 0 && aligned16(X) &&
                      aligned16(Y) && (!Z1 || (ldz1 % VN == 0 && aligned16(Z1))) &&
                      (!Z2 || (ldz2 % VN == 0 && aligned16(Z2)));
+    // narrow blocks (<= 8 chunks a row): 4 rows a thread and more CTAs per SM
+    // hide the L2 latency of the X window; wide blocks: 8 rows a thread
+    // amortise the window over more FMAs
+    if (vec && w / VN <= 8)
+        return launch_dia_kernel<T, kDiaR / 2, VN>(st, A, vals, w, X, ldx, Y, ldy, Z1, ldz1, Z2,
+                                                   ldz2, ca, cb, cc);
     if (vec)
         return launch_dia_kernel<T, kDiaR, VN>(st, A, vals, w, X, ldx, Y, ldy, Z1, ldz1, Z2,
                                                ldz2, ca, cb, cc);
