@@ -462,11 +462,14 @@ struct Solver {
 
     // algorithmic traffic of one SpMM of width w (A once, X once, extra
     // streamed operands once, Y written once)
+    // (over the DIA view: ndiag * n values, no indices)
     double spmm_bytes(int w, int extra) const {
         double vb = prec == CACG_MIXED ? 4.0 : 8.0;
-        return (double)A->nnz * (vb + 4.0) + 4.0 * (double)(A->n + 1) +
-               (double)A->n * w * (double)es() * (2.0 + extra);
+        const double xyz = (double)A->n * w * (double)es() * (2.0 + extra);
+        if (uses_dia()) return (double)A->dia_ndiag * (double)A->n * vb + xyz;
+        return (double)A->nnz * (vb + 4.0) + 4.0 * (double)(A->n + 1) + xyz;
     }
+    bool uses_dia() const { return p.spmm_format != CACG_SPMM_CSR && A->dia_ndiag > 0; }
 
     const void *val_t() const { return prec == CACG_MIXED ? (const void *)A->val32 : A->val; }
     size_t es() const { return prec == CACG_MIXED ? 4 : 8; }
@@ -476,7 +479,7 @@ struct Solver {
     template <typename T>
     int spmm(const T *X, int64_t ldx, T *Y, int64_t ldy, int w, const T *Z1, int64_t ldz1,
              const T *Z2, int64_t ldz2, double ca, double cb, double cc) {
-        if (p.spmm_format != CACG_SPMM_CSR && A->dia_ndiag > 0) {
+        if (uses_dia()) {
             int rc = launch_dia_spmm<T>(st, A, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc);
             if (rc != CACG_ERR_UNSUPPORTED) return rc;
         }
@@ -566,7 +569,9 @@ struct Solver {
     int residual(const double *B, const double *X, double *R, bool write_s0, double *norms) {
         const double dn = (double)A->n;
         prof.begin(CACG_PHASE_RESIDUAL,
-                   (double)A->nnz * 12.0 + 4.0 * (dn + 1) + dn * m * (8.0 * 3 + (double)es()),
+                   (uses_dia() ? (double)A->dia_ndiag * dn * 8.0
+                               : (double)A->nnz * 12.0 + 4.0 * (dn + 1)) +
+                       dn * m * (8.0 * 3 + (double)es()),
                    2.0 * (double)A->nnz * m);
         int rc;
         if (slices && write_s0) {
