@@ -192,6 +192,14 @@ int launch_qupdate_tc5(cudaStream_t st, int64_t n, int k, float *Qout, int64_t l
                        const float *Qin, int64_t ldq, const float *S, int64_t lds,
                        const double *beta, int *status);
 bool tsm_q_tc5_supported(int k);
+// X += Q alpha, R -= AQ alpha, S0 = R32 = (float)R, norms: tcgen05, m <= 16, k <= 256
+int launch_xrupdate_tc5(cudaStream_t st, int64_t n, int k, int m, const float *Q,
+                        const float *AQ, int64_t ldq, const double *alpha, double *X, double *R,
+                        float *S0, int64_t lds, float *R32, double *norms, double *ws,
+                        int *status);
+bool tsm_xr_tc5_supported(int k, int m);
+// norms[c] = sum over G partial rows of part[g * m + c] (fixed order)
+int launch_colsum(cudaStream_t st, const double *part, int G, int m, double *norms);
 int launch_split_planes(cudaStream_t st, int64_t n, int w, const float *X, int64_t ld,
                         Slices out);
 bool gram_tcs_supported(int ka, int kb1, int kb2, int64_t ldl, int64_t ldr1, int64_t ldr2);

@@ -269,6 +269,310 @@ __global__ void __launch_bounds__(kTsThreads, 1)
     }
 }
 
+// ---------------------------------------------------------------------------
+// X += Q alpha, R -= AQ alpha (Q, AQ: n x k FP32, alpha: k x m FP64, X, R: n x m
+// FP64), S0 = (float)R, R32 = (float)R, per-CTA partial ||R(:,c)||^2.
+// Reference: dense_distributedMatL_localMatR_Mul_v1 (src/BLAS3.c:794-825) for
+// Q alpha and AQ alpha, dense_mat_mat_add_TP (src/BLAS3.c:579-612) for the
+// updates, norm2square_dist_denseMat_col_n (src/MatrixOperations.c:110-142).
+// Same pipeline as the Q update; a tile takes 2 * KS steps (Q's K blocks, then
+// AQ's), the MMAs accumulate Q alpha and AQ alpha into adjacent TMEM column
+// ranges (N = 16 each, alpha zero-padded to 16 columns), and the epilogue
+// thread of a row applies both updates in FP64.
+constexpr int kXrN = 16;
+
+__global__ void __launch_bounds__(kTsThreads, 1)
+    tsm_xr_tc5_kernel(int64_t n, int K, int m, const float *__restrict__ Q,
+                      const float *__restrict__ AQ, int64_t ldq,
+                      const double *__restrict__ alpha, double *__restrict__ X,
+                      double *__restrict__ R, float *__restrict__ S0, int64_t lds,
+                      float *__restrict__ R32, double *__restrict__ part, int tmem_half,
+                      int *__restrict__ status) {
+    const int Kp = (K + 31) / 32 * 32;
+    const int KS = Kp / kTsKT;
+    const unsigned w_bytes = kXrN * Kp * 2;  // one slice of alpha^T (16 x Kp)
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *wsl = smem_raw;
+    unsigned char *asl = smem_raw + ((3 * w_bytes + 1023) & ~1023u);
+    float *ring = reinterpret_cast<float *>(asl + 2 * 3 * kTsABytes);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(ring + kTsStages * kTsM * kTsRingLd);
+    uint64_t *mma_done = mbar, *acc_full = mbar + 2, *acc_empty = mbar + 4;
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(mbar + 6);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    double *red = reinterpret_cast<double *>(mbar + 8);  // kTsEpi norm partials, then staging
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t ntiles = (n + kTsM - 1) / kTsM;
+    const int64_t my_tiles =
+        ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int SPT = 2 * KS;  // steps per tile
+    const int64_t nsteps = my_tiles * SPT;
+
+    // alpha^T slices: B row c (output column, zero for c >= m), K-major
+    for (int pidx = tid; pidx < kXrN * Kp / 2; pidx += kTsThreads) {
+        const int c = pidx / (Kp / 2), j = 2 * (pidx % (Kp / 2));
+        const float w0 = (c < m && j < K) ? (float)alpha[(size_t)j * m + c] : 0.f;
+        const float w1 = (c < m && j + 1 < K) ? (float)alpha[(size_t)(j + 1) * m + c] : 0.f;
+        unsigned hw, mw, lw;
+        t5_split2(w0, w1, hw, mw, lw);
+        const unsigned off = (((c >> 3) * (Kp / 8) + (j >> 3)) * 64 + (c & 7) * 8 + (j & 7)) * 2;
+        *reinterpret_cast<unsigned *>(wsl + off) = hw;
+        *reinterpret_cast<unsigned *>(wsl + w_bytes + off) = mw;
+        *reinterpret_cast<unsigned *>(wsl + 2 * w_bytes + off) = lw;
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            t5_mbar_init(&mma_done[i], 1);
+            t5_mbar_init(&acc_full[i], 1);
+            t5_mbar_init(&acc_empty[i], kTsEpi / 32);
+        }
+        *abort_flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         t5_smem_u32(tmem_slot)),
+                     "r"(2 * tmem_half));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    t5_fence_proxy_async();
+    t5_fence_before();
+    __syncthreads();
+    t5_fence_after();
+    const unsigned tmem = *tmem_slot;
+
+    if (warp < kTsProd / 32) {
+        // ================================ producers (as in the Q update)
+        auto issue_loads = [&](int64_t j) {
+            if (j < nsteps) {
+                float *dst = ring + (int)(j % kTsStages) * kTsM * kTsRingLd;
+                const int64_t tj = j / SPT;
+                const int idx = (int)(j % SPT);
+                const float *src = idx < KS ? Q : AQ;
+                const int64_t r0 = (blockIdx.x + tj * gridDim.x) * (int64_t)kTsM;
+                const int c0 = (idx % KS) * kTsKT;
+#pragma unroll
+                for (int v = 0; v < kTsM * kTsKT / 4 / kTsProd; ++v) {
+                    const int id = tid + v * kTsProd;
+                    const int r = id >> 3, c4 = id & 7;
+                    const int64_t row = r0 + r;
+                    const int col = c0 + 4 * c4;
+                    const bool ok = row < n && col < K;
+                    t5_cp16(dst + r * kTsRingLd + 4 * c4,
+                            ok ? (const void *)(src + row * ldq + col) : src, ok ? 16 : 0);
+                }
+            }
+            t5_cp_commit();
+        };
+        auto convert = [&](int stage, int buf) {
+            const float *src = ring + stage * kTsM * kTsRingLd;
+            unsigned char *dst = asl + buf * 3 * kTsABytes;
+#pragma unroll
+            for (int u = 0; u < kTsM * kTsKT / 8 / kTsProd; ++u) {
+                const int id = tid + u * kTsProd;
+                const int q = id & 7, o = (id >> 3) & 3, g = id >> 5;
+                const int row = 8 * g + q;
+                const float4 x0 = *reinterpret_cast<const float4 *>(src + row * kTsRingLd + 8 * o);
+                const float4 x1 =
+                    *reinterpret_cast<const float4 *>(src + row * kTsRingLd + 8 * o + 4);
+                unsigned hw[4], mw[4], lw[4];
+                t5_split2(x0.x, x0.y, hw[0], mw[0], lw[0]);
+                t5_split2(x0.z, x0.w, hw[1], mw[1], lw[1]);
+                t5_split2(x1.x, x1.y, hw[2], mw[2], lw[2]);
+                t5_split2(x1.z, x1.w, hw[3], mw[3], lw[3]);
+                const unsigned off = ((row >> 3) * (kTsKT / 8) + o) * 128 + (row & 7) * 16;
+                *reinterpret_cast<uint4 *>(dst + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(dst + kTsABytes + off) =
+                    make_uint4(mw[0], mw[1], mw[2], mw[3]);
+                *reinterpret_cast<uint4 *>(dst + 2 * kTsABytes + off) =
+                    make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+        };
+        constexpr unsigned idesc = t5_idesc(kTsM, kXrN);
+        auto issue_mma = [&](int64_t j) -> bool {
+            const int buf = (int)(j & 1);
+            const int64_t tj = j / SPT;
+            const int idx = (int)(j % SPT);
+            const int op = idx / KS, kc = idx % KS;
+            const int tb = (int)(tj & 1);
+            if (idx == 0 && tj >= 2) {
+                if (!t5_mbar_wait(&acc_empty[tb], (unsigned)(((tj - 2) >> 1) & 1))) return false;
+                t5_fence_after();
+            }
+            const unsigned d = tmem + (unsigned)(tb * tmem_half + op * kXrN);
+            const unsigned abase = t5_smem_u32(asl + buf * 3 * kTsABytes);
+            const unsigned wbase = t5_smem_u32(wsl);
+            unsigned accumulate = kc != 0;
+            const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+            for (int pr = 0; pr < 6; ++pr) {
+#pragma unroll
+                for (int kk = 0; kk < kTsKT / 16; ++kk) {
+                    if (kc * kTsKT + kk * 16 >= K) continue;  // K-padding half
+                    const uint64_t ad = t5_desc(abase + pa[pr] * kTsABytes + kk * 256, 512);
+                    const uint64_t bd = t5_desc(wbase + pb[pr] * w_bytes + (kc * 4 + kk * 2) * 128,
+                                                (unsigned)(Kp / 8) * 128);
+                    t5_mma(d, ad, bd, idesc, accumulate);
+                    accumulate = 1;
+                }
+            }
+            t5_commit(&mma_done[buf]);
+            if (idx == SPT - 1) t5_commit(&acc_full[tb]);
+            return true;
+        };
+
+        int timed_out = 0, aborted = 0;
+        int64_t last_committed = -1;
+        for (int j = 0; j < kTsStages - 1; ++j) issue_loads(j);
+        for (int64_t i = 0; i <= nsteps; ++i) {
+            if (i < nsteps) asm volatile("cp.async.wait_group %0;\n" ::"n"(kTsStages - 2));
+            t5_fence_proxy_async();
+            t5_fence_before();
+            aborted = t5_bar_or(1, kTsProd, timed_out);
+            t5_fence_after();
+            if (aborted) break;
+            if (i >= 1 && tid == 0) {
+                if (issue_mma(i - 1)) {
+                    last_committed = i - 1;
+                } else {
+                    atomicOr(status, kStatusTimeout);
+                    timed_out = 1;
+                }
+            }
+            if (i == nsteps) break;
+            issue_loads(i + kTsStages - 1);
+            if (i >= 2 && !__all_sync(0xffffffffu, t5_mbar_wait(&mma_done[i & 1],
+                                                                (unsigned)(((i - 2) >> 1) & 1)))) {
+                if (lane == 0) atomicOr(status, kStatusTimeout);
+                timed_out = 1;
+            }
+            convert((int)(i % kTsStages), (int)(i & 1));
+        }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        if (aborted && tid == 0) {
+            *abort_flag = 1;
+            if (last_committed >= 0)
+                t5_mbar_wait(&mma_done[last_committed & 1], (unsigned)((last_committed >> 1) & 1));
+        }
+    } else {
+        // ================================ epilogue: rows 32 * quad .. +31 of each tile.
+        // Lane l reads TMEM row l (the tcgen05.ld lane rule), the warp stages its
+        // 32 x m accumulator values in shared memory (row stride 17: conflict
+        // free) and then walks the rows cooperatively: element e = it * 32 + l
+        // is row e / m, column l % m (m divides 32), so X, R, S0, R32 accesses
+        // are contiguous across the warp and a lane keeps one column's norm.
+        const int quad = warp & 3, et = tid - kTsProd;
+        float *stg = reinterpret_cast<float *>(red + kTsEpi) + (size_t)quad * 2 * 32 * 17;
+        const int rpi = 32 / m;             // rows per warp step
+        const int lr = lane / m, lc = lane % m;
+        const bool lact = lr < rpi;          // lanes past rpi * m idle
+        double sq = 0.0;
+        for (int64_t tj = 0; tj < my_tiles; ++tj) {
+            const int64_t row0 = (blockIdx.x + tj * gridDim.x) * (int64_t)kTsM + 32 * quad;
+            double xv[kXrN], rw[kXrN];
+#pragma unroll
+            for (int it = 0; it < kXrN; ++it) {
+                const int64_t row = row0 + it * rpi + lr;
+                const bool ok = it < m && lact && row < n;
+                xv[it] = ok ? X[row * m + lc] : 0.0;
+                rw[it] = ok ? R[row * m + lc] : 0.0;
+            }
+            const int tb = (int)(tj & 1);
+            const bool ok = __all_sync(0xffffffffu, t5_mbar_wait_or_abort(
+                                                        &acc_full[tb], (unsigned)((tj >> 1) & 1),
+                                                        abort_flag));
+            if (!ok) {
+                if (lane == 0) {
+                    if (!*abort_flag) atomicOr(status, kStatusTimeout);
+                    *abort_flag = 1;
+                }
+                break;
+            }
+            t5_fence_after();
+            const unsigned tbase = tmem + ((unsigned)(32 * quad) << 16) + (unsigned)(tb * tmem_half);
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {  // D1 cols 0-7, 8-15, D2 cols 0-7, 8-15
+                float v[8];
+                t5_ld8(tbase + 8 * h, v);
+                float *dst = stg + (h >> 1) * 32 * 17 + lane * 17 + 8 * (h & 1);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) dst[q] = v[q];
+            }
+            t5_fence_before();
+            __syncwarp();
+            if (lane == 0) t5_mbar_arrive(&acc_empty[tb]);
+#pragma unroll
+            for (int it = 0; it < kXrN; ++it) {
+                const int r = it * rpi + lr;
+                const int64_t row = row0 + r;
+                if (it < m && lact && row < n) {
+                    const double x = xv[it] + (double)stg[r * 17 + lc];
+                    const double rr = rw[it] - (double)stg[32 * 17 + r * 17 + lc];
+                    X[row * m + lc] = x;
+                    R[row * m + lc] = rr;
+                    const float rf = (float)rr;
+                    if (S0) S0[row * lds + lc] = rf;
+                    if (R32) R32[row * m + lc] = rf;
+                    sq = fma(rr, rr, sq);
+                }
+            }
+            __syncwarp();  // staging area reused by the next tile
+        }
+        // fixed-order per-CTA norm partials: column c sums the lanes holding it
+        if (part) {
+            red[et] = lact ? sq : 0.0;
+            asm volatile("bar.sync 2, %0;\n" ::"n"(kTsEpi) : "memory");
+            if (et < m) {
+                double t = 0.0;
+                for (int q = 0; q < kTsEpi; ++q)
+                    if ((q & 31) < rpi * m && (q & 31) % m == et) t += red[q];
+                part[(size_t)blockIdx.x * m + et] = t;
+            }
+        }
+    }
+    t5_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        t5_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                     "r"(2 * tmem_half));
+    }
+}
+
+static size_t tsm_xr_smem(int k) {
+    const int Kp = (k + 31) / 32 * 32;
+    return (((size_t)3 * kXrN * Kp * 2 + 1023) & ~(size_t)1023) + 2 * 3 * (size_t)kTsABytes +
+           (size_t)kTsStages * kTsM * kTsRingLd * 4 + 8 * 8 + (size_t)kTsEpi * 8 +
+           (size_t)4 * 2 * 32 * 17 * 4;
+}
+
+bool tsm_xr_tc5_supported(int k, int m) {
+    return k >= 4 && k % 4 == 0 && k <= 256 && m >= 1 && m <= kXrN && 32 % m == 0 &&
+           tsm_xr_smem(k) <= max_smem_optin();
+}
+
+int launch_xrupdate_tc5(cudaStream_t st, int64_t n, int k, int m, const float *Q,
+                        const float *AQ, int64_t ldq, const double *alpha, double *X, double *R,
+                        float *S0, int64_t lds, float *R32, double *norms, double *ws,
+                        int *status) {
+    if (n < 0 || !alpha || !X || !R || !status || (norms && !ws)) return CACG_ERR_ARG;
+    if (!tsm_xr_tc5_supported(k, m) || ldq % 4 || !aligned16(Q) || !aligned16(AQ))
+        return CACG_ERR_UNSUPPORTED;
+    if (n == 0) return CACG_OK;
+    const size_t smem = tsm_xr_smem(k);
+    static const bool attr = [] {
+        cudaFuncSetAttribute(tsm_xr_tc5_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    const int64_t ntiles = (n + kTsM - 1) / kTsM;
+    const int grid = (int)std::min<int64_t>(ntiles, sm_count());
+    tsm_xr_tc5_kernel<<<grid, kTsThreads, smem, st>>>(n, k, m, Q, AQ, ldq, alpha, X, R, S0, lds,
+                                                      R32, norms ? ws : nullptr, 32, status);
+    int rc = check_launch();
+    if (rc != CACG_OK || !norms) return rc;
+    return launch_colsum(st, ws, grid, m, norms);
+}
 static size_t tsm_q_smem(int k) {
     const int Kp = (k + 31) / 32 * 32;
     return 3 * (size_t)k * Kp * 2 + 2 * 3 * (size_t)kTsABytes +

@@ -247,6 +247,11 @@ __global__ void colsum_kernel(const double *__restrict__ part, int G, int m,
     out[c] = s;
 }
 
+int launch_colsum(cudaStream_t st, const double *part, int G, int m, double *norms) {
+    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(part, G, m, norms);
+    return check_launch();
+}
+
 size_t norm_workspace_doubles(int64_t n, int m) {
     (void)n;
     return (size_t)2048 * (size_t)(m > 0 ? m : 1);  // >= kRedBlocks and kXrMaxBlocks
@@ -926,6 +931,26 @@ extern "C" int cacg_k_gerschgorin(int64_t n, const int32_t *row_ptr, const int32
     return rc;
 }
 
+// Runs a launcher that reports bounded-wait expiry in a device status word;
+// maps the word to CACG_ERR_TIMEOUT (synchronises the stream).
+template <typename F>
+static int run_with_status(cudaStream_t st, F &&launch) {
+    int *dstat = nullptr;
+    if (cudaMallocAsync((void **)&dstat, sizeof(int), st) != cudaSuccess) return CACG_ERR_OOM;
+    cudaMemsetAsync(dstat, 0, sizeof(int), st);
+    int rc = launch(dstat);
+    int hstat = 0;
+    if (rc == CACG_OK) {
+        cudaMemcpyAsync(&hstat, dstat, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess)
+            rc = CACG_ERR_CUDA;
+        else if (hstat & kStatusTimeout)
+            rc = CACG_ERR_TIMEOUT;
+    }
+    cudaFreeAsync(dstat, st);
+    return rc;
+}
+
 extern "C" int cacg_k_qupdate(int32_t vtype, int64_t n, int32_t k, void *Q, int64_t ldq,
                               const void *S, int64_t lds, const double *beta, void *stream) {
     // in place on Q: the product reads all of Q's row, so stage a copy first
@@ -943,21 +968,10 @@ extern "C" int cacg_k_qupdate(int32_t vtype, int64_t n, int32_t k, void *Q, int6
         rc = launch_qupdate<float>(st, n, k, (float *)Q, ldq, (const float *)Qin, ldq,
                                    (const float *)S, lds, beta);
     } else if (vtype == (CACG_VAL_F32 | CACG_VAL_TC5)) {
-        int *dstat = nullptr;
-        if (cudaMallocAsync((void **)&dstat, sizeof(int), st) != cudaSuccess) {
-            cudaFreeAsync(Qin, st);
-            return CACG_ERR_OOM;
-        }
-        cudaMemsetAsync(dstat, 0, sizeof(int), st);
-        rc = launch_qupdate_tc5(st, n, k, (float *)Q, ldq, (const float *)Qin, ldq,
-                                (const float *)S, lds, beta, dstat);
-        int hstat = 0;
-        if (rc == CACG_OK) {
-            cudaMemcpyAsync(&hstat, dstat, sizeof(int), cudaMemcpyDeviceToHost, st);
-            if (cudaStreamSynchronize(st) != cudaSuccess) rc = CACG_ERR_CUDA;
-            else if (hstat & kStatusTimeout) rc = CACG_ERR_TIMEOUT;
-        }
-        cudaFreeAsync(dstat, st);
+        rc = run_with_status(st, [&](int *dstat) {
+            return launch_qupdate_tc5(st, n, k, (float *)Q, ldq, (const float *)Qin, ldq,
+                                      (const float *)S, lds, beta, dstat);
+        });
     } else {
         rc = CACG_ERR_ARG;
     }
@@ -990,6 +1004,11 @@ extern "C" int cacg_k_xrupdate(int32_t vtype, int64_t n, int32_t k, int32_t m, c
                    : launch_xrupdate_fast<float>(st, n, k, m, (const float *)Q,
                                                  (const float *)AQ, ldq, alpha, X, R,
                                                  (float *)S0, lds, nullptr, norms, ws);
+    else if (vtype == (CACG_VAL_F32 | CACG_VAL_TC5) && !exact)
+        rc = run_with_status(st, [&](int *dstat) {
+            return launch_xrupdate_tc5(st, n, k, m, (const float *)Q, (const float *)AQ, ldq, alpha,
+                                       X, R, (float *)S0, lds, nullptr, norms, ws, dstat);
+        });
     else
         rc = CACG_ERR_ARG;
     cudaFreeAsync(ws, st);

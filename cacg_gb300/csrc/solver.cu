@@ -21,9 +21,11 @@
 // Precision modes:
 //   CACG_FP64   all FP64 (parity mode with the reference).
 //   CACG_MIXED  A, S, Q, AQ in FP32 (SpMM and basis in FP32); Gram products
-//               accumulated FP64-accurately; LU, alpha, beta, X, R in FP64;
-//               R = B - A X recomputed in FP64 every rr_period iterations and
-//               before convergence is declared.
+//               and Q = S - Q beta on the tcgen05 tensor cores (bf16x3 slices,
+//               FP32 accumulation, Gram group sums in float-float, split-K in
+//               FP64); LU, alpha, beta, X, R in FP64; R = B - A X recomputed in
+//               FP64 every rr_period iterations and before convergence is
+//               declared.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -737,6 +739,8 @@ struct Solver {
         if (prec == CACG_MIXED && p.exact_updates)
             return launch_xrupdate<T>(st, A->n, k, m, Q, AQ, k, b.alpha, X, b.R, (T *)b.S, k,
                                       b.R32, b.norms, b.norm_ws);
+        // (the tcgen05 X/R update, launch_xrupdate_tc5, is slower than the
+        // CUDA-core kernel at m = 16: its N = 16 MMAs are latency-bound)
         return launch_xrupdate_fast<T>(st, A->n, k, m, Q, AQ, k, b.alpha, X, b.R, (T *)b.S, k,
                                        b.R32, b.norms, b.norm_ws);
     }

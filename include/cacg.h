@@ -72,11 +72,12 @@ extern "C" {
 #define CACG_VAL_F64 0
 #define CACG_VAL_F32 1
 #define CACG_XR_EXACT 16 /* or-ed into cacg_k_xrupdate's vtype: float-float sums */
-#define CACG_VAL_TC5 32  /* or-ed into cacg_k_qupdate's vtype (FP32 only): the product
-                            on the 5th-generation tensor cores (three bf16 slices per
-                            value, six slice products, FP32 accumulation); returns
-                            CACG_ERR_UNSUPPORTED unless k is a multiple of 16, k <= 96,
-                            and the rows are 16-byte aligned */
+#define CACG_VAL_TC5 32  /* or-ed into the vtype of cacg_k_qupdate / cacg_k_xrupdate
+                            (FP32 only): the products on the 5th-generation tensor
+                            cores (three bf16 slices per value, six slice products,
+                            FP32 accumulation).  Returns CACG_ERR_UNSUPPORTED outside
+                            qupdate: k % 16 == 0, k <= 96; xrupdate: k % 4 == 0,
+                            k <= 256, m <= 16 dividing 32; both: 16-byte aligned rows */
 
 /* generators (cacg_gen_*) */
 #define CACG_GEN_LAPLACE2D_5PT 1

@@ -254,6 +254,47 @@ def test_xrupdate(lib, torch_cuda, vt, exact, n, k, m):
     assert relerr(host(norms), (Rg * Rg).sum(axis=0)) <= 1e-13
 
 
+@pytest.mark.parametrize("n,k,m", [(10000, 64, 8), (20000, 96, 16), (777, 4, 1),
+                                   (3000, 20, 4), (4000, 256, 16), (130001, 96, 16),
+                                   (5001, 32, 2)])
+def test_xrupdate_tcgen05(lib, torch_cuda, n, k, m):
+    """X += Q alpha, R -= AQ alpha with the products on the tcgen05 tensor
+    cores (bf16x3 slices, FP32 accumulation; X, R updated in FP64): within
+    the FP32-product tolerance of the CUDA-core kernel; S0 = (float)R; norms
+    of the new R in FP64."""
+    torch = torch_cuda
+    Q = O.gen_rhs("normal", n, k, 1).astype(np.float32)
+    AQ = O.gen_rhs("normal", n, k, 2).astype(np.float32)
+    al = O.gen_rhs("normal", k, m, 3)
+    X = O.gen_rhs("normal", n, m, 4)
+    R = O.gen_rhs("normal", n, m, 5)
+    Xw = X + O.port_tallsmall(Q.astype(np.float64), al)
+    Rw = R - O.port_tallsmall(AQ.astype(np.float64), al)
+    dQ, dAQ, dal, dX, dR = (dev(torch, a) for a in (Q, AQ, al, X, R))
+    S0 = torch.zeros((n, k), dtype=torch.float32, device="cuda")
+    norms = torch.zeros(m, dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_xrupdate(F32 | TC5, n, k, m, ptr(dQ), ptr(dAQ), k, ptr(dal), ptr(dX),
+                             ptr(dR), ptr(S0), k, ptr(norms), None)
+    assert rc == 0
+    assert relerr(host(dX), Xw) <= 5e-6
+    assert relerr(host(dR), Rw) <= 5e-6
+    Rg = host(dR)
+    assert relerr(host(S0)[:, :m], Rg) <= 1e-7
+    assert relerr(host(norms), (Rg * Rg).sum(axis=0)) <= 1e-13
+
+
+@pytest.mark.parametrize("m", [32, 5])
+def test_xrupdate_tcgen05_rejects_unsupported_widths(lib, torch_cuda, m):
+    torch = torch_cuda
+    n, k = 100, 64
+    z = lambda *sh, dt=torch.float32: torch.zeros(sh, dtype=dt, device="cuda")
+    rc = lib.cacg_k_xrupdate(F32 | TC5, n, k, m, ptr(z(n, k)), ptr(z(n, k)), k,
+                             ptr(z(k, m, dt=torch.float64)), ptr(z(n, m, dt=torch.float64)),
+                             ptr(z(n, m, dt=torch.float64)), ptr(z(n, k)), k,
+                             ptr(z(m, dt=torch.float64)), None)
+    assert rc == -6
+
+
 @pytest.mark.parametrize("k,r", [(4, 1), (64, 64), (64, 8), (96, 96), (96, 16), (128, 32),
                                  (200, 20), (256, 32)])
 def test_lu_matches_reference(lib, torch_cuda, k, r):
