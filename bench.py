@@ -37,11 +37,14 @@ WORKLOADS = {
     # the headline configuration (3-D 27-point 128^3, 16 RHS)
     "st27_128_m16": dict(kind="st3d27", N=128, m=16, s=6, rhs="uniform", seed=2, a=-1.0,
                          b=1.0, bounds=("given", 0.05, 52.0), rr=5, tol=1e-8),
+    # the same family at 96^3 (n = 884,736): the size of the ncu captures
+    "st27_96_m16": dict(kind="st3d27", N=96, m=16, s=6, rhs="uniform", seed=2, a=-1.0,
+                        b=1.0, bounds=("given", 0.05, 52.0), rr=5, tol=1e-8),
     # a small instance of the same family (for quick checks)
     "st27_32_m16": dict(kind="st3d27", N=32, m=16, s=6, rhs="uniform", seed=2, a=-1.0,
                         b=1.0, bounds=("given", 0.05, 52.0), rr=5, tol=1e-8),
 }
-CPU_SAMPLE_N = {"st27_128_m16": 48, "st27_32_m16": 16}
+CPU_SAMPLE_N = {"st27_128_m16": 48, "st27_96_m16": 40, "st27_32_m16": 16}
 
 
 def reduce_max(x: float, world: int, device=None) -> float:

@@ -288,22 +288,48 @@ __global__ void __launch_bounds__(512)
 }
 
 // C[a][b] = sum over chunks p (in order) of part[p][tile(a,b)][a%BA][b%BB]
-__global__ void gram_reduce_kernel(const double *__restrict__ part, int nchunks, int ntiles,
-                                   int BA, int BB, int tilesB, int ka, int kb, int kb1,
-                                   double *__restrict__ C1, int ldc1, double *__restrict__ C2,
-                                   int ldc2) {
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= ka * kb) return;
-    int a = idx / kb, b = idx % kb;
-    int tile = (a / BA) * tilesB + (b / BB);
-    size_t off = (size_t)tile * BA * BB + (size_t)(a % BA) * BB + (b % BB);
-    size_t stride = (size_t)ntiles * BA * BB;
+// C = sum over chunks of the per-chunk partial tiles.  Four threads share one
+// output element: thread quarter q sums its contiguous quarter of the chunks
+// in chunk order (loads issued 8 at a time, coalesced across elements), then
+// quarter 0 adds the four quarter sums in quarter order -- a fixed order
+// that depends only on the shape.
+constexpr int kRedElems = 64;  // output elements per block (x 4 quarters = 256 threads)
+
+__global__ void __launch_bounds__(4 * kRedElems)
+    gram_reduce_kernel(const double *__restrict__ part, int nchunks, int ntiles, int BA, int BB,
+                       int tilesB, int ka, int kb, int kb1, double *__restrict__ C1, int ldc1,
+                       double *__restrict__ C2, int ldc2) {
+    __shared__ double qs[4][kRedElems];
+    const int el = threadIdx.x % kRedElems, q = threadIdx.x / kRedElems;
+    const int idx = blockIdx.x * kRedElems + el;
+    const bool active = idx < ka * kb;
+    const int a = active ? idx / kb : 0, b = active ? idx % kb : 0;
+    const int tile = (a / BA) * tilesB + (b / BB);
+    const size_t off = (size_t)tile * BA * BB + (size_t)(a % BA) * BB + (b % BB);
+    const size_t stride = (size_t)ntiles * BA * BB;
+    const int per = (nchunks + 3) / 4;
+    const int p0 = q * per, p1 = min(nchunks, p0 + per);
     double s = 0.0;
-    for (int p = 0; p < nchunks; ++p) s += part[off + (size_t)p * stride];
-    if (b < kb1)
-        C1[(size_t)a * ldc1 + b] = s;
-    else
-        C2[(size_t)a * ldc2 + (b - kb1)] = s;
+    if (active) {
+        int p = p0;
+        for (; p + 8 <= p1; p += 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = part[off + (size_t)(p + u) * stride];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += v[u];
+        }
+        for (; p < p1; ++p) s += part[off + (size_t)p * stride];
+    }
+    qs[q][el] = s;
+    __syncthreads();
+    if (q == 0 && active) {
+        const double t = ((qs[0][el] + qs[1][el]) + qs[2][el]) + qs[3][el];
+        if (b < kb1)
+            C1[(size_t)a * ldc1 + b] = t;
+        else
+            C2[(size_t)a * ldc2 + (b - kb1)] = t;
+    }
 }
 
 struct GramPlan {
@@ -413,7 +439,7 @@ int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl
         cudaMemsetAsync(ws, 0, need, st);
     }
     int tot = ka * kb;
-    gram_reduce_kernel<<<(tot + 255) / 256, 256, 0, st>>>(ws, n > 0 ? p.nchunks : 1,
+    gram_reduce_kernel<<<(tot + kRedElems - 1) / kRedElems, 4 * kRedElems, 0, st>>>(ws, n > 0 ? p.nchunks : 1,
                                                           p.tilesA * p.tilesB, p.BA, p.BB,
                                                           p.tilesB, ka, kb, kb1, C1, ldc1,
                                                           C2, ldc2);
@@ -424,8 +450,8 @@ int launch_gram_reduce(cudaStream_t st, const double *part, int nchunks, int nti
                        int BB, int tilesB, int ka, int kb, int kb1, double *C1, int ldc1,
                        double *C2, int ldc2) {
     int tot = ka * kb;
-    gram_reduce_kernel<<<(tot + 255) / 256, 256, 0, st>>>(part, nchunks, ntiles, BA, BB, tilesB,
-                                                          ka, kb, kb1, C1, ldc1, C2, ldc2);
+    gram_reduce_kernel<<<(tot + kRedElems - 1) / kRedElems, 4 * kRedElems, 0, st>>>(
+        part, nchunks, ntiles, BA, BB, tilesB, ka, kb, kb1, C1, ldc1, C2, ldc2);
     return check_launch();
 }
 
@@ -646,7 +672,7 @@ static int gram_fixed_scratch(cudaStream_t st, int variant, int64_t n, const T *
         if (cudaMemsetAsync(ws, 0, need, st) != cudaSuccess) return CACG_ERR_CUDA;
     }
     int tot = ka * kb;
-    gram_reduce_kernel<<<(tot + 255) / 256, 256, 0, st>>>(ws, n > 0 ? p.nchunks : 1,
+    gram_reduce_kernel<<<(tot + kRedElems - 1) / kRedElems, 4 * kRedElems, 0, st>>>(ws, n > 0 ? p.nchunks : 1,
                                                           p.tilesA * p.tilesB, p.BA, p.BB,
                                                           p.tilesB, ka, kb, kb1, C1, ldc1,
                                                           C2, ldc2);

@@ -108,6 +108,89 @@ __global__ void __launch_bounds__(kLuRC * kLuTPC)
     }
 }
 
+// Column-sweep ("axpy") triangular solves, one warp per right-hand side:
+// lane l owns rows l, l+32, ...; at forward step i the owner's value times
+// the stored reciprocal pivot is y_i, broadcast with one shuffle, and every
+// lane subtracts L[j][i] y_i from its rows j > i; the backward sweep does the
+// same with the unit upper factor.  The factor is staged transposed in shared
+// memory (FT[i][j] = F[j][i]), so step i reads row i of FT, conflict-free.
+// Same arithmetic as the substitution above, summed column by column
+// (agrees with the reference to rounding).  T = ceil(k / 32) rows per lane.
+constexpr int kLuWarpsPerCta = 2;
+
+template <int T>
+__global__ void __launch_bounds__(32 * kLuWarpsPerCta)
+    lu_solve_sweep_kernel(int k, const double *__restrict__ F, int r,
+                          const double *__restrict__ RHS, double *__restrict__ Y) {
+    extern __shared__ __align__(16) double FT[];  // k * k transposed, then k reciprocal pivots
+    double *Dinv = FT + (size_t)k * k;
+    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
+        const int j = idx / k, i = idx % k;
+        FT[(size_t)i * k + j] = F[idx];
+    }
+    for (int i = threadIdx.x; i < k; i += blockDim.x) Dinv[i] = F[(size_t)k * k + i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kLuWarpsPerCta + (threadIdx.x >> 5);
+    if (c >= r) return;  // no block-wide barrier follows
+    double z[T];
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
+        const int j = lane + 32 * t;
+        z[t] = j < k ? RHS[(size_t)j * r + c] : 0.0;
+    }
+    // forward: y_i = z_i / L_ii; z_j -= L_ji y_i (j > i)
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
+        for (int ii = 0; ii < 32; ++ii) {
+            const int i = 32 * t + ii;
+            if (i >= k) break;
+            const double yi = __shfl_sync(0xffffffffu, z[t], ii) * Dinv[i];
+            if (lane == ii) z[t] = yi;
+            const double *col = FT + (size_t)i * k;
+#pragma unroll
+            for (int tt = t; tt < T; ++tt) {
+                const int j = lane + 32 * tt;
+                if (j > i && j < k) z[tt] = fma(-col[j], yi, z[tt]);
+            }
+        }
+    }
+    // backward (U unit diagonal): x_i = z_i; z_j -= U_ji x_i (j < i)
+#pragma unroll
+    for (int t = T - 1; t >= 0; --t) {
+        for (int ii = 31; ii >= 0; --ii) {
+            const int i = 32 * t + ii;
+            if (i >= k) continue;
+            const double xi = __shfl_sync(0xffffffffu, z[t], ii);
+            const double *col = FT + (size_t)i * k;
+#pragma unroll
+            for (int tt = 0; tt <= t; ++tt) {
+                const int j = lane + 32 * tt;
+                if (j < i) z[tt] = fma(-col[j], xi, z[tt]);
+            }
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
+        const int j = lane + 32 * t;
+        if (j < k) Y[(size_t)j * r + c] = z[t];
+    }
+}
+
+template <int T>
+static int launch_sweep(cudaStream_t st, int k, const double *F, int r, const double *RHS,
+                        double *Y, size_t smem) {
+    static const bool attr = [] {
+        cudaFuncSetAttribute(lu_solve_sweep_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    const int blocks = (r + kLuWarpsPerCta - 1) / kLuWarpsPerCta;
+    lu_solve_sweep_kernel<T><<<blocks, 32 * kLuWarpsPerCta, smem, st>>>(k, F, r, RHS, Y);
+    return check_launch();
+}
+
 int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *status) {
     if (k <= 0) return CACG_ERR_ARG;
     int use_smem = k <= kLuSmemK;
@@ -125,6 +208,18 @@ int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *st
 int launch_lu_solve(cudaStream_t st, int k, const double *F, int r, const double *RHS,
                     double *Y) {
     if (k <= 0 || r <= 0) return CACG_ERR_ARG;
+    {
+        const size_t sweep_smem = ((size_t)k * k + k) * sizeof(double);
+        if (k <= 160 && sweep_smem <= max_smem_optin()) {
+            switch ((k + 31) / 32) {
+                case 1: return launch_sweep<1>(st, k, F, r, RHS, Y, sweep_smem);
+                case 2: return launch_sweep<2>(st, k, F, r, RHS, Y, sweep_smem);
+                case 3: return launch_sweep<3>(st, k, F, r, RHS, Y, sweep_smem);
+                case 4: return launch_sweep<4>(st, k, F, r, RHS, Y, sweep_smem);
+                case 5: return launch_sweep<5>(st, k, F, r, RHS, Y, sweep_smem);
+            }
+        }
+    }
     size_t zbytes = (size_t)k * kLuRC * sizeof(double);
     size_t fbytes = ((size_t)k * k + k) * sizeof(double);
     int use_smem = (fbytes + zbytes) <= max_smem_optin() - 1024;

@@ -238,17 +238,28 @@ __global__ void __launch_bounds__(kRowThreads)
 }
 
 // out[c] = sum over g < G of part[g*m + c]; non-finite -> status bit
-__global__ void colsum_kernel(const double *__restrict__ part, int G, int m,
-                              double *__restrict__ out) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= m) return;
+// out[c] = sum over g of part[g * m + c]: one block per column, each thread
+// sums a strided subset in g order, then a fixed shared-memory tree.
+constexpr int kColsumThreads = 256;
+
+__global__ void __launch_bounds__(kColsumThreads)
+    colsum_kernel(const double *__restrict__ part, int G, int m, double *__restrict__ out) {
+    __shared__ double red[kColsumThreads];
+    const int c = blockIdx.x;
     double s = 0.0;
-    for (int g = 0; g < G; ++g) s += part[(size_t)g * m + c];
-    out[c] = s;
+    for (int g = threadIdx.x; g < G; g += kColsumThreads) s += part[(size_t)g * m + c];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kColsumThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[c] = red[0];
 }
 
 int launch_colsum(cudaStream_t st, const double *part, int G, int m, double *norms) {
-    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(part, G, m, norms);
+    if (m <= 0) return CACG_OK;
+    colsum_kernel<<<m, kColsumThreads, 0, st>>>(part, G, m, norms);
     return check_launch();
 }
 
@@ -287,8 +298,7 @@ int launch_xrupdate(cudaStream_t st, int64_t n, int k, int m, const T *Q, const 
                                                      lds, R32, norms ? ws : nullptr);
     int rc = check_launch();
     if (rc != CACG_OK || !norms) return rc;
-    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G, m, norms);
-    return check_launch();
+    return launch_colsum(st, ws, G, m, norms);
 }
 
 template int launch_xrupdate<double>(cudaStream_t, int64_t, int, int, const double *,
@@ -409,8 +419,7 @@ int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, c
                                                            lds, R32, norms ? ws : nullptr);
     int rc = check_launch();
     if (rc != CACG_OK || !norms) return rc;
-    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G2, m, norms);
-    return check_launch();
+    return launch_colsum(st, ws, G2, m, norms);
 }
 
 template int launch_xrupdate_fast<double>(cudaStream_t, int64_t, int, int, const double *,
@@ -648,8 +657,7 @@ int launch_xrupdate_direct(cudaStream_t st, int64_t n, int k, int m, const T *Q,
         n, k, m, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms ? ws : nullptr, s0sl, r32sl);
     int rc = check_launch();
     if (rc != CACG_OK || !norms) return rc;
-    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, (int)blocks, m, norms);
-    return check_launch();
+    return launch_colsum(st, ws, (int)blocks, m, norms);
 }
 
 // ------------------------------------------------------ residual epilogue
@@ -712,8 +720,7 @@ int launch_residual_post(cudaStream_t st, int64_t n, int m, double *R, void *S0,
                                                           nullptr, norms ? ws : nullptr);
     rc = check_launch();
     if (rc != CACG_OK || !norms) return rc;
-    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G, m, norms);
-    return check_launch();
+    return launch_colsum(st, ws, G, m, norms);
 }
 
 int launch_colnorm(cudaStream_t st, int64_t n, int m, const double *R, double *norms,
@@ -727,8 +734,7 @@ int launch_colnorm(cudaStream_t st, int64_t n, int m, const double *R, double *n
     rowpost_kernel<double><<<G, kRowThreads, 0, st>>>(n, m, mp, R, nullptr, 0, nullptr, ws);
     int rc = check_launch();
     if (rc != CACG_OK) return rc;
-    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G, m, norms);
-    return check_launch();
+    return launch_colsum(st, ws, G, m, norms);
 }
 
 int launch_residual_sl(cudaStream_t st, int64_t n, const int32_t *rp, const int32_t *ci,
@@ -748,8 +754,7 @@ int launch_residual_sl(cudaStream_t st, int64_t n, const int32_t *rp, const int3
                                                      norms ? ws : nullptr, S0sl, R32sl);
     rc = check_launch();
     if (rc != CACG_OK || !norms) return rc;
-    colsum_kernel<<<(m + 127) / 128, 128, 0, st>>>(ws, G, m, norms);
-    return check_launch();
+    return launch_colsum(st, ws, G, m, norms);
 }
 
 int launch_qupdate_sl(cudaStream_t st, int64_t n, int k, float *Qout, int64_t ldo,
@@ -897,7 +902,7 @@ int launch_dot(cudaStream_t st, int64_t n, const double *a, const double *b, dou
     dot_kernel<<<G, kRowThreads, 0, st>>>(n, a, b, ws);
     int rc = check_launch();
     if (rc != CACG_OK) return rc;
-    colsum_kernel<<<1, 32, 0, st>>>(ws, G, 1, out);
+    colsum_kernel<<<1, kColsumThreads, 0, st>>>(ws, G, 1, out);
     return check_launch();
 }
 
