@@ -11,8 +11,9 @@
 // for alpha, and one iteration later for beta); here the factor of each
 // Q^T AQ is computed once and reused by both solves.
 //
-// The factor F is k*k + k doubles: the Crout factors, then the reciprocals
-// of L's diagonal (the reference multiplies by 1/L_ii, src/DLSsolvers.c:168).
+// The factor F is 2*k*k + k doubles: the Crout factors, the reciprocals of
+// L's diagonal (the reference multiplies by 1/L_ii, src/DLSsolvers.c:168),
+// and the factors again, transposed, for the column-sweep solves.
 // A zero or non-finite pivot sets *status = 1 (CACG_ERR_BREAKDOWN at the
 // host) instead of trapping; the arithmetic continues as the reference's
 // does (inf/NaN propagate) and the host stops the iteration.
@@ -48,15 +49,23 @@ __global__ void __launch_bounds__(kLuThreads)
             for (int c = d + 1 + threadIdx.x; c < k; c += 32) W[d * k + c] *= inv;
         }
         __syncthreads();
-        const int t = k - d - 1;
-        for (int q = threadIdx.x; q < t * t; q += blockDim.x) {
-            int i = d + 1 + q / t, c = d + 1 + q % t;
-            W[i * k + c] = W[i * k + c] - W[i * k + d] * W[d * k + c];
+        // trailing update, rows by warp, columns by lane (no index division)
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int i = d + 1 + warp; i < k; i += kLuThreads / 32) {
+            const double lid = W[i * k + d];
+            for (int c = d + 1 + lane; c < k; c += 32)
+                W[i * k + c] = W[i * k + c] - lid * W[d * k + c];
         }
         __syncthreads();
     }
     if (use_smem)
         for (int i = threadIdx.x; i < kk; i += blockDim.x) F[i] = W[i];
+    // transposed copy for the column-sweep solves: FT[i][j] = F[j][i]
+    double *FT = F + (size_t)kk + k;
+    for (int idx = threadIdx.x; idx < kk; idx += blockDim.x) {
+        const int i = idx / k, j = idx % k;
+        FT[idx] = W[(size_t)j * k + i];
+    }
     if (threadIdx.x == 0 && bad && status) atomicOr(status, kStatusBreakdown);
 }
 
@@ -124,9 +133,22 @@ __global__ void __launch_bounds__(32 * kLuWarpsPerCta)
                           const double *__restrict__ RHS, double *__restrict__ Y) {
     extern __shared__ __align__(16) double FT[];  // k * k transposed, then k reciprocal pivots
     double *Dinv = FT + (size_t)k * k;
-    for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) {
-        const int j = idx / k, i = idx % k;
-        FT[(size_t)i * k + j] = F[idx];
+    {
+        // the factor kernel wrote FT after F and the pivots: contiguous copy,
+        // 16-byte loads issued 8 at a time (k (k + 1) is even: aligned)
+        const double2 *src = reinterpret_cast<const double2 *>(F + (size_t)k * k + k);
+        double2 *dst = reinterpret_cast<double2 *>(FT);
+        const int n2 = k * k / 2;
+        int q = threadIdx.x;
+        for (; q + 7 * (int)blockDim.x < n2; q += 8 * blockDim.x) {
+            double2 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = src[q + u * blockDim.x];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) dst[q + u * blockDim.x] = v[u];
+        }
+        for (; q < n2; q += blockDim.x) dst[q] = src[q];
+        if ((k * k) & 1 && threadIdx.x == 0) FT[k * k - 1] = F[(size_t)k * k + k + k * k - 1];
     }
     for (int i = threadIdx.x; i < k; i += blockDim.x) Dinv[i] = F[(size_t)k * k + i];
     __syncthreads();
@@ -244,7 +266,7 @@ extern "C" int cacg_k_lu(int32_t k, const double *M, int32_t r, const double *RH
                          int *status, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     double *F = nullptr;
-    if (cudaMallocAsync((void **)&F, ((size_t)k * k + k) * sizeof(double), st) != cudaSuccess)
+    if (cudaMallocAsync((void **)&F, ((size_t)2 * k * k + k) * sizeof(double), st) != cudaSuccess)
         return CACG_ERR_OOM;
     int rc = launch_lu_factor(st, k, M, F, status);
     if (rc == CACG_OK) rc = launch_lu_solve(st, k, F, r, RHS, Y);

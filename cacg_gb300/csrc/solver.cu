@@ -173,9 +173,9 @@ static Layout layout(int64_t n, int m, int s, int prec, bool lanczos, bool slice
     L.R32 = prec == CACG_MIXED ? align256((size_t)n * m * 4) : 0;
     L.Ssl = slices ? align256((size_t)3 * n * k * 2) : 0;
     L.R32sl = slices ? align256((size_t)3 * n * m * 2) : 0;
-    // small: QtAS k*k, QtAQ k*k, QtR k*m, F k*k, alpha k*m, beta k*k, norms m,
+    // small: QtAS k*k, QtAQ k*k, QtR k*m, F 2*k*k + k, alpha k*m, beta k*k, norms m,
     //        bnorm m, true norms m, bounds 2, scalars 16, status (int) 16
-    L.small = align256(sizeof(double) * ((size_t)4 * k * k + k + (size_t)2 * k * m +
+    L.small = align256(sizeof(double) * ((size_t)5 * k * k + k + (size_t)2 * k * m +
                                          3 * (size_t)m + 64));
     L.gram = align256(std::max(
         gram_workspace_bytes(n, k, k + m),
@@ -391,7 +391,7 @@ static void carve(char *base, const Layout &L, int m, int k, SolveBuffers *b) {
     double *sm = (double *)(base + L.o_small);
     b->QtAS = sm; sm += (size_t)k * k;
     b->QtAQ = sm; sm += (size_t)k * k;
-    b->F = sm; sm += (size_t)k * k + k;
+    b->F = sm; sm += (size_t)2 * k * k + k;  // factors, pivot reciprocals, factors transposed
     b->beta = sm; sm += (size_t)k * k;
     b->QtR = sm; sm += (size_t)k * m;
     b->alpha = sm; sm += (size_t)k * m;
