@@ -20,6 +20,7 @@ TOL_ABS_COL0, TOL_REL_ALL = 0, 1
 FP64, MIXED = 0, 1
 GRAM_AUTO, GRAM_FMA, GRAM_DMMA, GRAM_TC, GRAM_TC_SLICES, GRAM_TC5 = 0, 1, 2, 3, 4, 5
 SPMM_AUTO, SPMM_CSR = 0, 1
+RESID_AUTO, RESID_FP64 = 0, 1
 VAL_F64, VAL_F32 = 0, 1
 
 
@@ -36,7 +37,7 @@ class CacgParams(C.Structure):
                 ("gram_variant", C.c_int32), ("lanczos_seed", C.c_uint64),
                 ("stream", C.c_void_p), ("use_graph", C.c_int32),
                 ("exact_updates", C.c_int32), ("spmm_format", C.c_int32),
-                ("reserved", C.c_int32 * 5)]
+                ("residual_precision", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 class CacgResult(C.Structure):

@@ -34,7 +34,8 @@ struct DevMatrix {
     int64_t dia_npad = 0;
     DiaDesc dia{};
     double *dia64 = nullptr;
-    float *dia32 = nullptr;
+    float *dia32 = nullptr;    // FP32 values (hi) ...
+    float *dia32lo = nullptr;  // ... and val - hi, same allocation
     size_t owned_bytes = 0;
     cudaStream_t st = nullptr;  // stream of the stream-ordered allocations
     static int create(const cacg_csr *A, bool want_f32, DevMatrix *M, cudaStream_t st);
@@ -42,6 +43,15 @@ struct DevMatrix {
     int ensure_f32(cudaStream_t st);
     void release();
 };
+
+int launch_dia_hilo(cudaStream_t st, int64_t count, const double *v64, float *hi, float *lo);
+int launch_ff_split(cudaStream_t st, int64_t count, const double *x, float *hi, float *lo);
+// R = B - A X in float-float over the DIA view, with S0 = R32 = (float)R and
+// the column norms of R; Xh, Xl: n x m FP32 scratch (k_dia.cu)
+int launch_dia_residual_ff(cudaStream_t st, const DevMatrix *A, int m, const double *X,
+                           const double *B, double *R, float *Xh, float *Xl, float *S0,
+                           int64_t lds, float *R32, double *norms, double *ws,
+                           int64_t ws_doubles);
 
 // Y = ca A X + cb Z1 + cc Z2 over the DIA view (k_dia.cu);
 // CACG_ERR_UNSUPPORTED when the matrix has no view of this precision.

@@ -64,7 +64,12 @@ __global__ void dia_fill_kernel(int64_t n, int64_t npad, const int32_t *__restri
                 return;
             }
             v64[(size_t)d * npad + row] = val[p];
-            if (v32) v32[(size_t)d * npad + row] = (float)val[p];
+            if (v32) {  // FP32 view: hi, then lo = val - hi (float-float residuals)
+                const float hi = (float)val[p];
+                v32[(size_t)d * npad + row] = hi;
+                v32[(size_t)desc.ndiag * npad + (size_t)d * npad + row] =
+                    (float)(val[p] - (double)hi);
+            }
         }
     }
 }
@@ -157,7 +162,7 @@ int DevMatrix::build_dia(const cacg_csr *A, bool want_f32, cudaStream_t st) {
     }
     desc.gstart[desc.ngroups] = nd;
     const int64_t npad = (n + kDiaR - 1) / kDiaR * kDiaR + kDiaR;
-    const size_t b64 = (size_t)nd * npad * 8, b32 = want_f32 ? (size_t)nd * npad * 4 : 0;
+    const size_t b64 = (size_t)nd * npad * 8, b32 = want_f32 ? (size_t)2 * nd * npad * 4 : 0;
     double *v64 = nullptr;
     float *v32 = nullptr;
     int *bad = nullptr;
@@ -193,9 +198,81 @@ int DevMatrix::build_dia(const cacg_csr *A, bool want_f32, cudaStream_t st) {
     dia_npad = npad;
     dia64 = v64;
     dia32 = v32;
+    dia32lo = v32 ? v32 + (size_t)nd * npad : nullptr;
     dia_ndiag = nd;
     owned_bytes += b64 + b32;
     return CACG_OK;
+}
+
+// -------------------------------------------------------------- float-float
+// x = hi + lo with FP32 hi, lo, using integer operations only (GB300's FP64
+// pipe runs at 1/64 of the FP32 rate): hi = x truncated to 24 significant
+// bits, lo = the next 29 bits rounded to FP32 (about 48 bits in all).
+// Values outside the normal FP32 exponent range give (float)x, 0.
+__device__ __forceinline__ void ff_split_bits(double x, float &hi, float &lo) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FF);
+    const unsigned long long sgn = b >> 63;
+    if (e < 1023 - 126 + 24 || e > 1023 + 127) {  // tiny, huge, inf, NaN, zero
+        hi = (float)x;
+        lo = 0.f;
+        return;
+    }
+    const unsigned long long mant = b & ((1ull << 52) - 1);
+    hi = __uint_as_float((unsigned)((sgn << 31) | ((unsigned long long)(e - 1023 + 127) << 23) |
+                                    (mant >> 29)));
+    const unsigned rem = (unsigned)(mant & ((1u << 29) - 1));
+    // rem * 2^(e - 1075): the scale is a normal FP32 power of two in this range
+    const int se = e - 1075 + 127;
+    const float scale = se >= 1 ? __uint_as_float((unsigned)se << 23) : 0.f;
+    const float l = __uint2float_rn(rem) * scale;
+    lo = sgn ? -l : l;
+}
+
+// exact FP32 -> FP64 by bits for normal values (others through the cast)
+__device__ __forceinline__ double ff_widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFF;
+    if (e == 0 || e == 0xFF) return (double)f;
+    const unsigned long long b = ((unsigned long long)(u >> 31) << 63) |
+                                 ((unsigned long long)(e - 127 + 1023) << 52) |
+                                 ((unsigned long long)(u & 0x7FFFFF) << 29);
+    return __longlong_as_double((long long)b);
+}
+
+__global__ void ff_split_kernel(int64_t count, const double *__restrict__ x,
+                                float *__restrict__ hi, float *__restrict__ lo) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float h, l;
+        ff_split_bits(x[i], h, l);
+        hi[i] = h;
+        lo[i] = l;
+    }
+}
+
+int launch_ff_split(cudaStream_t st, int64_t count, const double *x, float *hi, float *lo) {
+    if (count <= 0) return CACG_OK;
+    const int blocks = (int)std::min<int64_t>((count + 255) / 256, (int64_t)sm_count() * 16);
+    ff_split_kernel<<<blocks, 256, 0, st>>>(count, x, hi, lo);
+    return check_launch();
+}
+
+// FP32 hi/lo view from the FP64 view (matrices created without FP32 values)
+__global__ void dia_hilo_kernel(int64_t count, const double *__restrict__ v64,
+                                float *__restrict__ hi, float *__restrict__ lo) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float h = (float)v64[i];
+        hi[i] = h;
+        lo[i] = (float)(v64[i] - (double)h);
+    }
+}
+
+int launch_dia_hilo(cudaStream_t st, int64_t count, const double *v64, float *hi, float *lo) {
+    const int blocks = (int)std::min<int64_t>((count + 255) / 256, (int64_t)sm_count() * 16);
+    dia_hilo_kernel<<<blocks, 256, 0, st>>>(count, v64, hi, lo);
+    return check_launch();
 }
 
 // -------------------------------------------------------------- SpMM
@@ -375,6 +452,207 @@ static int launch_dia_kernel(cudaStream_t st, const DevMatrix *A, const T *vals,
         A->n, A->dia_npad, A->dia, vals, cpr, runs_per_block, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2,
         ca, cb, cc);
     return check_launch();
+}
+
+// R = B - A X in float-float arithmetic over the DIA view (mixed mode's
+// residual replacement), with the residual post-pass fused in:
+// S0 = R32 = (float)R, per-block partial ||R(:,c)||^2.  A = hi + lo (FP32
+// views), X = Xh + Xl (ff_split_bits); each term a x is p + e + t with
+// p = ah xh, e its exact FMA error, t = ah xl + al xh; the row sum is kept
+// as (sh, sl) with TwoSum (about 2^-44 relative); B - sum is formed in
+// float-float and widened to FP64 with one FP64 add.  Same thread layout as
+// dia_spmm_kernel (R rows x 4 columns per thread, hi and lo values of the
+// next row block staged in shared memory); m % 4 == 0.
+__device__ __forceinline__ void ff_mac(float &sh, float &sl, float ah, float al, float xh,
+                                       float xl) {
+    const float p = ah * xh;
+    const float e = fmaf(ah, xh, -p);
+    const float t = fmaf(ah, xl, fmaf(al, xh, e));
+    const float s = sh + p;
+    const float bp = s - sh;
+    const float err = (sh - (s - bp)) + (p - bp);
+    sh = s;
+    sl += err + t;
+}
+
+template <int R>
+__global__ void __launch_bounds__(kDiaThreads, 2)
+    dia_resid_ff_kernel(int64_t n, int64_t npad, DiaDesc desc, const float *__restrict__ vals,
+                        int cpr, int runs_per_block, const float *__restrict__ Xh,
+                        const float *__restrict__ Xl, int m, const double *__restrict__ B,
+                        double *__restrict__ Rout, float *__restrict__ S0, int64_t lds,
+                        float *__restrict__ R32, double *__restrict__ part) {
+    constexpr int CW = 4;
+    constexpr int W = R + kDiaGroupMax - 1;
+    extern __shared__ __align__(16) unsigned char dia_smem[];
+    float *vs = reinterpret_cast<float *>(dia_smem);  // [2][2 nd][BR]: hi rows, then lo rows
+    const int lr = threadIdx.x / cpr, c = threadIdx.x % cpr;
+    const bool active = lr < runs_per_block;
+    const int BR = runs_per_block * R;
+    const int64_t nblk = (n + BR - 1) / BR;
+    const int nd = desc.ndiag, nd2 = 2 * nd;  // vals: hi view, then lo view (nd * npad apart)
+
+    auto stage = [&](int64_t blk, int buf) {
+        if (blk < nblk) {
+            float *dst = vs + (size_t)buf * nd2 * BR;
+            const int per = BR / 4;
+            const int dstep = blockDim.x / per, qstep = blockDim.x % per;
+            int d = threadIdx.x / per, q = threadIdx.x % per;
+            for (; d < nd2; d += dstep, q += qstep) {
+                if (q >= per) {
+                    q -= per;
+                    ++d;
+                    if (d >= nd2) break;
+                }
+                const int64_t e0 = blk * BR + (int64_t)q * 4;
+                const int64_t left = npad - e0;
+                const int by = left >= 4 ? 16 : (left > 0 ? (int)left * 4 : 0);
+                dia_cp16(dst + (size_t)d * BR + q * 4,
+                         by ? (const void *)(vals + (size_t)d * npad + e0) : vals, by);
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::);
+    };
+
+    double sq[CW] = {0.0, 0.0, 0.0, 0.0};
+    int buf = 0;
+    stage(blockIdx.x, 0);
+    for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x, buf ^= 1) {
+        stage(blk + gridDim.x, buf ^ 1);
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncthreads();
+        if (active) {
+            const int64_t r0 = blk * BR + (int64_t)lr * R;
+            float ah_[R][CW], al_[R][CW];
+#pragma unroll
+            for (int i = 0; i < R; ++i)
+#pragma unroll
+                for (int q = 0; q < CW; ++q) ah_[i][q] = al_[i][q] = 0.f;
+            for (int g = 0; g < desc.ngroups; ++g) {
+                const int d0 = desc.gstart[g], G = desc.gstart[g + 1] - d0;
+                const int64_t x0 = r0 + desc.off[d0];
+                float wh[W][CW], wl[W][CW];
+#pragma unroll
+                for (int t = 0; t < W; ++t) {
+                    if (t < R + G - 1) {
+                        int64_t xr = x0 + t;
+                        xr = xr < 0 ? 0 : (xr >= n ? n - 1 : xr);  // value is 0 there
+                        vload(wh[t], Xh + xr * m + (int64_t)c * CW);
+                        vload(wl[t], Xl + xr * m + (int64_t)c * CW);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < kDiaGroupMax; ++j) {
+                    if (j < G) {
+                        float vh[R], vl[R];
+                        const float *ph = vs + ((size_t)buf * nd2 + d0 + j) * BR + lr * R;
+                        const float *pl = ph + (size_t)nd * BR;
+#pragma unroll
+                        for (int i = 0; i < R; i += 4) {
+                            float t4[4];
+                            vload_plain(t4, ph + i);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) vh[i + u] = t4[u];
+                            vload_plain(t4, pl + i);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) vl[i + u] = t4[u];
+                        }
+#pragma unroll
+                        for (int i = 0; i < R; ++i)
+#pragma unroll
+                            for (int q = 0; q < CW; ++q)
+                                ff_mac(ah_[i][q], al_[i][q], vh[i], vl[i], wh[i + j][q],
+                                       wl[i + j][q]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+                const int64_t row = r0 + i;
+                if (row >= n) break;
+                const int64_t col = (int64_t)c * CW;
+                const double2 b01 = *reinterpret_cast<const double2 *>(B + row * m + col);
+                const double2 b23 = *reinterpret_cast<const double2 *>(B + row * m + col + 2);
+                const double bv[CW] = {b01.x, b01.y, b23.x, b23.y};
+                double rd[CW];
+                float rf[CW];
+#pragma unroll
+                for (int q = 0; q < CW; ++q) {
+                    float bh, bl;
+                    ff_split_bits(bv[q], bh, bl);
+                    // (bh + bl) - (sh + sl) in float-float
+                    const float sh = ah_[i][q], sl = al_[i][q];
+                    const float s = bh - sh;
+                    const float bp = s - bh;
+                    const float err = (bh - (s - bp)) + (-sh - bp);
+                    const float lo = err + (bl - sl);
+                    rd[q] = ff_widen(s) + ff_widen(lo);
+                    rf[q] = s + lo;
+                    const double w = ff_widen(rf[q]);
+                    sq[q] = fma(w, w, sq[q]);
+                }
+                *reinterpret_cast<double2 *>(Rout + row * m + col) = make_double2(rd[0], rd[1]);
+                *reinterpret_cast<double2 *>(Rout + row * m + col + 2) = make_double2(rd[2], rd[3]);
+                if (S0) vstore(S0 + row * lds + col, rf);
+                if (R32) vstore(R32 + row * m + col, rf);
+            }
+        }
+        __syncthreads();  // buffer `buf` is refilled two blocks on
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    // per-block column partials in fixed order (runs ascending); staging reused
+    if (part) {
+        __syncthreads();
+        double *red = reinterpret_cast<double *>(dia_smem);  // runs_per_block x m
+        if (active)
+#pragma unroll
+            for (int q = 0; q < CW; ++q) red[(size_t)lr * m + c * CW + q] = sq[q];
+        __syncthreads();
+        for (int col = threadIdx.x; col < m; col += blockDim.x) {
+            double t = 0.0;
+            for (int r = 0; r < runs_per_block; ++r) t += red[(size_t)r * m + col];
+            part[(size_t)blockIdx.x * m + col] = t;
+        }
+    }
+}
+
+// Float-float residual (see above); CACG_ERR_UNSUPPORTED when the matrix has
+// no FP32 hi/lo view or m is not a multiple of 4.  Xh, Xl: n x m scratch.
+int launch_dia_residual_ff(cudaStream_t st, const DevMatrix *A, int m, const double *X,
+                           const double *B, double *R, float *Xh, float *Xl, float *S0,
+                           int64_t lds, float *R32, double *norms, double *ws,
+                           int64_t ws_doubles) {
+    if (!A || A->dia_ndiag <= 0 || !A->dia32 || !A->dia32lo || m % 4 != 0 || m <= 0)
+        return CACG_ERR_UNSUPPORTED;
+    if (!aligned16(X) || !aligned16(B) || !aligned16(R) || !aligned16(Xh) || !aligned16(Xl) ||
+        (S0 && (lds % 4 || !aligned16(S0))) || (R32 && !aligned16(R32)))
+        return CACG_ERR_UNSUPPORTED;
+    constexpr int RR = kDiaR / 2;
+    const int cpr = m / 4;
+    if (cpr > kDiaThreads) return CACG_ERR_UNSUPPORTED;
+    const int runs_per_block = std::min(kDiaThreads / cpr, std::max(1, 512 / RR));
+    const int BR = runs_per_block * RR;
+    const size_t smem = std::max((size_t)2 * 2 * A->dia_ndiag * BR * 4,
+                                 (size_t)runs_per_block * m * 8);
+    if (smem > 200 * 1024) return CACG_ERR_UNSUPPORTED;
+    const int64_t nblk = (A->n + BR - 1) / BR;
+    const int per_sm = std::max(1, std::min(2, (int)(220 * 1024 / smem)));
+    const int64_t blocks = std::min<int64_t>(nblk, (int64_t)sm_count() * per_sm);
+    if (norms && (int64_t)blocks * m > ws_doubles) return CACG_ERR_UNSUPPORTED;
+    int rc = launch_ff_split(st, A->n * (int64_t)m, X, Xh, Xl);
+    if (rc != CACG_OK) return rc;
+    static const bool attr = [] {
+        cudaFuncSetAttribute(dia_resid_ff_kernel<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
+        return true;
+    }();
+    (void)attr;
+    dia_resid_ff_kernel<RR><<<(unsigned)blocks, kDiaThreads, smem, st>>>(
+        A->n, A->dia_npad, A->dia, A->dia32, cpr, runs_per_block, Xh, Xl, m, B, R, S0, lds, R32,
+        norms ? ws : nullptr);
+    rc = check_launch();
+    if (rc != CACG_OK || !norms) return rc;
+    return launch_colsum(st, ws, (int)blocks, m, norms);
 }
 
 template <typename T>

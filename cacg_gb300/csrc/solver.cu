@@ -120,9 +120,10 @@ int DevMatrix::ensure_f32(cudaStream_t st) {
     }
     if (dia_ndiag > 0 && !dia32) {
         const int64_t cnt = (int64_t)dia_ndiag * dia_npad;
-        CACG_CUDA_TRY(cudaMallocAsync((void **)&dia32, (size_t)cnt * 4, st));
-        owned_bytes += (size_t)cnt * 4;
-        return launch_cast_f64_f32(st, cnt, dia64, dia32);
+        CACG_CUDA_TRY(cudaMallocAsync((void **)&dia32, (size_t)cnt * 8, st));
+        owned_bytes += (size_t)cnt * 8;
+        dia32lo = dia32 + cnt;
+        return launch_dia_hilo(st, cnt, dia64, dia32, dia32lo);
     }
     return CACG_OK;
 }
@@ -140,6 +141,7 @@ void DevMatrix::release() {
     val32 = nullptr;
     dia64 = nullptr;
     dia32 = nullptr;
+    dia32lo = nullptr;
     dia_ndiag = 0;
     owned_bytes = 0;
 }
@@ -148,8 +150,8 @@ void DevMatrix::release() {
 static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct Layout {
-    size_t S, Q, AQ, R, R32, Bnorm, small, gram, norm, lanczos, total;
-    size_t o_S, o_Q, o_AQ, o_R, o_R32, o_small, o_gram, o_norm, o_lanczos;
+    size_t S, Q, AQ, R, R32, Xff, Bnorm, small, gram, norm, lanczos, total;
+    size_t o_S, o_Q, o_AQ, o_R, o_R32, o_Xff, o_small, o_gram, o_norm, o_lanczos;
     size_t Ssl, R32sl, o_Ssl, o_Qsl, o_AQsl, o_R32sl;
     bool slices;
 };
@@ -171,6 +173,7 @@ static Layout layout(int64_t n, int m, int s, int prec, bool lanczos, bool slice
     L.S = L.Q = L.AQ = align256((size_t)n * k * es + 64);
     L.R = align256((size_t)n * m * 8);
     L.R32 = prec == CACG_MIXED ? align256((size_t)n * m * 4) : 0;
+    L.Xff = prec == CACG_MIXED ? align256((size_t)n * m * 8) : 0;  // X as FP32 hi, lo
     L.Ssl = slices ? align256((size_t)3 * n * k * 2) : 0;
     L.R32sl = slices ? align256((size_t)3 * n * m * 2) : 0;
     // small: QtAS k*k, QtAQ k*k, QtR k*m, F 2*k*k + k, alpha k*m, beta k*k, norms m,
@@ -191,6 +194,7 @@ static Layout layout(int64_t n, int m, int s, int prec, bool lanczos, bool slice
     L.o_AQ = o; o += L.AQ;
     L.o_R = o; o += L.R;
     L.o_R32 = o; o += L.R32;
+    L.o_Xff = o; o += L.Xff;
     L.o_small = o; o += L.small;
     L.o_gram = o; o += L.gram;
     L.o_norm = o; o += L.norm;
@@ -378,6 +382,8 @@ struct SolveBuffers {
     double *gram_ws;
     size_t gram_ws_bytes;
     double *norm_ws;
+    int64_t norm_ws_doubles;
+    float *Xff;  // n x m hi, then n x m lo (mixed mode's float-float residual)
     double *lz;  // 3 x n (Lanczos)
     Slices Ssl, Qsl, AQsl, R32sl;  // bf16 slice planes (mixed mode, when enabled)
 };
@@ -388,6 +394,7 @@ static void carve(char *base, const Layout &L, int m, int k, SolveBuffers *b) {
     b->AQ = base + L.o_AQ;
     b->R = (double *)(base + L.o_R);
     b->R32 = L.R32 ? (float *)(base + L.o_R32) : nullptr;
+    b->Xff = L.Xff ? (float *)(base + L.o_Xff) : nullptr;
     double *sm = (double *)(base + L.o_small);
     b->QtAS = sm; sm += (size_t)k * k;
     b->QtAQ = sm; sm += (size_t)k * k;
@@ -404,6 +411,7 @@ static void carve(char *base, const Layout &L, int m, int k, SolveBuffers *b) {
     b->gram_ws = (double *)(base + L.o_gram);
     b->gram_ws_bytes = L.gram;
     b->norm_ws = (double *)(base + L.o_norm);
+    b->norm_ws_doubles = (int64_t)((L.norm - 4096) / sizeof(double));
     b->lz = L.lanczos ? (double *)(base + L.o_lanczos) : nullptr;
 }
 
@@ -568,14 +576,30 @@ struct Solver {
     // residual replacement / true-residual checks.
     bool slices = false;
 
-    int residual(const double *B, const double *X, double *R, bool write_s0, double *norms) {
+    // R = B - A X.  ff: in the mixed mode over a DIA view, float-float
+    // arithmetic (FP32 pipe) instead of FP64 -- used for the periodic residual
+    // replacements; convergence checks and the reported residual use FP64.
+    int residual(const double *B, const double *X, double *R, bool write_s0, double *norms,
+                 bool ff = false) {
         const double dn = (double)A->n;
+        ff = ff && prec == CACG_MIXED && uses_dia() && !slices && b.Xff &&
+             p.residual_precision != CACG_RESID_FP64;
         prof.begin(CACG_PHASE_RESIDUAL,
-                   (uses_dia() ? (double)A->dia_ndiag * dn * 8.0
+                   (uses_dia() ? (double)A->dia_ndiag * dn * 8.0  // FP64, or FP32 hi + lo
                                : (double)A->nnz * 12.0 + 4.0 * (dn + 1)) +
                        dn * m * (8.0 * 3 + (double)es()),
                    2.0 * (double)A->nnz * m);
         int rc;
+        if (ff) {
+            rc = launch_dia_residual_ff(st, A, m, X, B, R, b.Xff, b.Xff + (size_t)A->n * m,
+                                        write_s0 ? (float *)b.S : nullptr, k,
+                                        write_s0 ? b.R32 : nullptr, norms, b.norm_ws,
+                                        b.norm_ws_doubles);
+            if (rc != CACG_ERR_UNSUPPORTED) {
+                prof.end();
+                return rc;
+            }
+        }
         if (slices && write_s0) {
             rc = launch_residual_sl(st, A->n, A->rp, A->ci, A->val, m, X, B, R, (float *)b.S, k,
                                     b.R32, norms, b.norm_ws, avg_nnz, b.Ssl, b.R32sl);
@@ -783,7 +807,7 @@ struct Solver {
             CACG_CUDA_TRY(cudaStreamSynchronize(st));
             for (int c = 0; c < m; ++c) bn[c] = h_pin[c] > 0 ? sqrt(h_pin[c]) : 1.0;
         }
-        rc = residual(B, X, b.R, true, b.norms);
+        rc = residual(B, X, b.R, true, b.norms, true);
         if (rc) return rc;
 
         auto rel_max = [&](const double *nr) {
@@ -828,7 +852,7 @@ struct Solver {
                     break;
                 }
                 if (prec == CACG_MIXED && p.rr_period > 0 && since_rr >= p.rr_period) {
-                    rc = residual(B, X, b.R, true, b.norms);
+                    rc = residual(B, X, b.R, true, b.norms, true);
                     if (rc) return rc;
                     res->residual_replacements++;
                     since_rr = 0;
@@ -839,7 +863,9 @@ struct Solver {
             bool rec_ok = rel_max(h_pin) <= p.tol;
             bool rr_due = prec == CACG_MIXED && p.rr_period > 0 && since_rr >= p.rr_period;
             if (rec_ok || rr_due) {
-                rc = residual(B, X, b.R, true, b.norms);
+                // a convergence check runs in FP64; a periodic replacement
+                // may run in float-float
+                rc = residual(B, X, b.R, true, b.norms, !rec_ok);
                 if (rc) return rc;
                 res->residual_replacements++;
                 since_rr = 0;

@@ -64,6 +64,7 @@ class Params:
     stream: int = 0
     exact_updates: bool = False     # mixed: float-float X/R update products
     spmm_format: str = "auto"       # "auto" (DIA view when the matrix has one) | "csr"
+    residual: str = "auto"          # mixed: "auto" (float-float replacements on DIA) | "fp64"
 
     def to_c(self) -> L.CacgParams:
         p = L.CacgParams()
@@ -90,6 +91,7 @@ class Params:
         p.stream = self.stream or None
         p.exact_updates = 1 if self.exact_updates else 0
         p.spmm_format = {"auto": L.SPMM_AUTO, "csr": L.SPMM_CSR}[self.spmm_format]
+        p.residual_precision = {"auto": L.RESID_AUTO, "fp64": L.RESID_FP64}[self.residual]
         return p
 
 

@@ -69,6 +69,9 @@ extern "C" {
 #define CACG_SPMM_AUTO 0
 #define CACG_SPMM_CSR 1 /* always the CSR kernels */
 
+#define CACG_RESID_AUTO 0
+#define CACG_RESID_FP64 1 /* residual replacements in FP64 as well */
+
 #define CACG_VAL_F64 0
 #define CACG_VAL_F32 1
 #define CACG_XR_EXACT 16 /* or-ed into cacg_k_xrupdate's vtype: float-float sums */
@@ -119,7 +122,11 @@ typedef struct cacg_params {
                               instead of FP32 FMAs */
     int32_t spmm_format;  /* CACG_SPMM_*: AUTO uses the matrix's DIA view when it
                              has one (results bit-identical to CSR) */
-    int32_t reserved[5];
+    int32_t residual_precision; /* CACG_RESID_*: MIXED with a DIA view computes the
+                                   periodic residual replacements in float-float
+                                   (about 44 bits, FP32 pipe) unless FP64 is asked
+                                   for; convergence checks are always FP64 */
+    int32_t reserved[4];
 } cacg_params;
 
 typedef struct cacg_result {

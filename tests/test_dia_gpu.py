@@ -29,7 +29,9 @@ def test_dia_solve_bit_identical_to_csr(lib, kind, N, ndiag, m, s, prec):
     B = cg.gen_rhs("normal", n, m, 3)
     M = cg.Matrix(rp, ci, v, want_fp32=True)
     assert M.diagonals() == ndiag
-    kw = dict(s=s, bounds="gerschgorin", tol=1e-8, maxit=400, precision=prec)
+    # FP64 residual replacements on both paths (the float-float replacement
+    # exists only over the DIA view)
+    kw = dict(s=s, bounds="gerschgorin", tol=1e-8, maxit=400, precision=prec, residual="fp64")
     Xd, idia = _solve_dev(M, B, cg.Params(spmm_format="auto", **kw))
     Xc, icsr = _solve_dev(M, B, cg.Params(spmm_format="csr", **kw))
     M.close()
@@ -79,3 +81,22 @@ def test_dia_view_found_on_large_grids(lib, kind, N, ndiag):
     M = cg.Matrix(rp, ci, v)
     assert M.diagonals() == ndiag
     M.close()
+
+
+@pytest.mark.parametrize("kind,N,m", [("st3d27", 24, 16), ("lap3d7", 20, 8), ("lap2d", 48, 4)])
+def test_float_float_residual_replacement(lib, kind, N, m):
+    """Mixed mode over a DIA view: periodic residual replacements in
+    float-float reach the same tolerance as FP64 replacements, with the
+    solutions within the solution tolerance and iteration counts within 2."""
+    rp, ci, v = cg.gen_matrix(kind, N, shift=1e-3)
+    n = len(rp) - 1
+    B = cg.gen_rhs("uniform", n, m, 9, -1.0, 1.0)
+    M = cg.Matrix(rp, ci, v, want_fp32=True)
+    kw = dict(s=4, bounds="gerschgorin", tol=1e-10, maxit=600, precision="mixed", rr_period=3)
+    Xf, inf_ = _solve_dev(M, B, cg.Params(residual="auto", **kw))
+    Xd, ind = _solve_dev(M, B, cg.Params(residual="fp64", **kw))
+    M.close()
+    assert inf_["status"] == 0 and ind["status"] == 0
+    assert inf_["true_relres_max"] <= 1e-10 and ind["true_relres_max"] <= 1e-10
+    assert abs(inf_["iterations"] - ind["iterations"]) <= 2
+    assert np.linalg.norm(Xf - Xd) <= 1e-7 * np.linalg.norm(Xd)
