@@ -372,6 +372,52 @@ struct Profiler {
     }
 };
 
+// Two captured outer iterations (one per buffer parity), replayed with
+// cudaGraphLaunch; launches inside a replay are added to the launch count.
+struct GraphPair {
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    int64_t kernels[2] = {0, 0};
+    template <class F>
+    int capture(cudaStream_t st, int par, F &&body) {
+        const int64_t l0 = g_launches.load();
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return CACG_ERR_CUDA;
+        }
+        const int rc = body();
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(st, &g);
+        kernels[par] = g_launches.load() - l0;
+        if (rc != CACG_OK || e != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return rc != CACG_OK ? rc : CACG_ERR_CUDA;
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&exec[par], g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            exec[par] = nullptr;
+            cudaGetLastError();
+            return CACG_ERR_CUDA;
+        }
+        // the capture recorded the launches; run them
+        g_launches -= kernels[par];
+        return replay(st, par);
+    }
+    int replay(cudaStream_t st, int par) {
+        if (cudaGraphLaunch(exec[par], st) != cudaSuccess) {
+            cudaGetLastError();
+            return CACG_ERR_CUDA;
+        }
+        g_launches += kernels[par];
+        return CACG_OK;
+    }
+    ~GraphPair() {
+        for (auto &e : exec)
+            if (e) cudaGraphExecDestroy(e);
+    }
+};
+
 // ----------------------------------------------------------- the solver
 struct SolveBuffers {
     void *S, *Q, *AQ;
@@ -822,8 +868,34 @@ struct Solver {
         int since_rr = 0;
         bool converged = false;
         int it = 0;
+        // CUDA graphs (use_graph, on a non-default stream): from iteration 2 on,
+        // an outer iteration's launch sequence is captured once per parity
+        // (Q and S swap buffers every iteration, so even and odd iterations
+        // differ only in which buffer is which) and replayed; the host repeats
+        // the buffer swap the captured iteration made.  Iterations 0 and 1 run
+        // uncaptured (iteration 0 differs, and every kernel's one-time setup
+        // happens outside a capture).
+        const bool graphs = p.use_graph != 0 && st != nullptr;
+        GraphPair gp;
+        const bool prof_on = prof.on;
         for (it = 0; it < p.maxit; ++it) {
-            rc = prec == CACG_MIXED ? iterate_once<float>(it, X) : iterate_once<double>(it, X);
+            if (graphs && it >= 2) {
+                const int par = it & 1;
+                prof.on = false;
+                if (!gp.exec[par]) {
+                    rc = gp.capture(st, par, [&] {
+                        return prec == CACG_MIXED ? iterate_once<float>(it, X)
+                                                  : iterate_once<double>(it, X);
+                    });
+                } else {
+                    std::swap(b.Q, b.S);
+                    std::swap(b.Qsl, b.Ssl);
+                    rc = gp.replay(st, par);
+                }
+                prof.on = prof_on;
+            } else {
+                rc = prec == CACG_MIXED ? iterate_once<float>(it, X) : iterate_once<double>(it, X);
+            }
             if (rc) return rc;
             int stv = 0;
             rc = fetch_norms(&stv);

@@ -117,7 +117,8 @@ typedef struct cacg_params {
     int32_t gram_variant; /* CACG_GRAM_* */
     uint64_t lanczos_seed;
     void *stream;         /* cudaStream_t, NULL = the library's own stream */
-    int32_t use_graph;    /* capture the outer iteration in a CUDA graph */
+    int32_t use_graph;    /* on a non-default stream: capture the outer iteration
+                             (from the third on) in CUDA graphs and replay them */
     int32_t exact_updates; /* MIXED: X/R update products summed in float-float
                               instead of FP32 FMAs */
     int32_t spmm_format;  /* CACG_SPMM_*: AUTO uses the matrix's DIA view when it
