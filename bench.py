@@ -311,16 +311,17 @@ def run_gpu_arm(args, w, rank, world):
 
     # end to end through the C ABI with host buffers (cacg_solve): A, B and
     # the initial X go host->device, X comes back, every step
+    # the caller's X (in/out, as cbcg_v1's X) is reset to x0 = 0 every step
     Xh = np.zeros_like(B)
     hb = 4 * (n + 1) + 12 * nnz + 2 * 8 * n * m
     db = 8 * n * m
-    _X, _ = cg.solve(rp, ci, v, B, Xh, params=pm)  # warm-up
+    _X, _ = cg.solve(rp, ci, v, B, Xh, params=pm, overwrite_x0=True)  # warm-up
     k_e2e = max(1, min(args.steps, 3))
     barrier()
     t0 = time.perf_counter()
     for _ in range(k_e2e):
-        Xh = np.zeros_like(B)
-        Xe, ie = cg.solve(rp, ci, v, B, Xh, params=pm)
+        Xh.fill(0.0)
+        Xe, ie = cg.solve(rp, ci, v, B, Xh, params=pm, overwrite_x0=True)
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / k_e2e
     assert ie["true_relres_max"] <= w["tol"]

@@ -1168,8 +1168,8 @@ int cacg_solve(const cacg_csr *A, const double *B, double *X, int32_t m, const c
     int rc = DevMatrix::create(A, p->precision == CACG_MIXED, &M, st);
     double *dB = nullptr, *dX = nullptr;
     size_t bytes = (size_t)A->n * m * sizeof(double);
-    if (rc == CACG_OK && cudaMalloc((void **)&dB, bytes) != cudaSuccess) rc = CACG_ERR_OOM;
-    if (rc == CACG_OK && cudaMalloc((void **)&dX, bytes) != cudaSuccess) rc = CACG_ERR_OOM;
+    if (rc == CACG_OK && cudaMallocAsync((void **)&dB, bytes, st) != cudaSuccess) rc = CACG_ERR_OOM;
+    if (rc == CACG_OK && cudaMallocAsync((void **)&dX, bytes, st) != cudaSuccess) rc = CACG_ERR_OOM;
     if (rc == CACG_OK) {
         cudaMemcpyAsync(dB, B, bytes, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(dX, X, bytes, cudaMemcpyHostToDevice, st);
@@ -1182,9 +1182,10 @@ int cacg_solve(const cacg_csr *A, const double *B, double *X, int32_t m, const c
         }
         rc = r2;
     }
-    if (dB) cudaFree(dB);
-    if (dX) cudaFree(dX);
+    if (dB) cudaFreeAsync(dB, st);
+    if (dX) cudaFreeAsync(dX, st);
     M.release();
+    cudaStreamSynchronize(st);
     cudaGetLastError();
     res->status = rc;
     return rc;

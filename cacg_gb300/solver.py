@@ -113,14 +113,26 @@ def _csr(rp, ci, v):
     return A, (rp, ci, v)
 
 
-def solve(rp, ci, v, B, X0=None, params: Params | None = None, **kw):
-    """Solve A X = B on the GPU (host arrays in and out).  Returns (X, info)."""
+def solve(rp, ci, v, B, X0=None, params: Params | None = None, overwrite_x0: bool = False,
+          **kw):
+    """Solve A X = B on the GPU (host arrays in and out).  Returns (X, info).
+
+    overwrite_x0=True solves in place in X0 (a C-contiguous float64 n x m
+    array, the reference's in/out X of cbcg_v1/bcbcg_v1): no host copy of the
+    initial guess, the returned X is X0 itself."""
     params = params or Params(**kw)
     B = np.ascontiguousarray(B, np.float64)
     if B.ndim == 1:
         B = B[:, None]
     n, m = B.shape
-    X = np.zeros_like(B) if X0 is None else np.array(X0, np.float64, order="C", copy=True)
+    if overwrite_x0:
+        if not (isinstance(X0, np.ndarray) and X0.dtype == np.float64 and X0.shape == (n, m)
+                and X0.flags["C_CONTIGUOUS"] and X0.flags["WRITEABLE"]):
+            raise ValueError("overwrite_x0 needs X0 as a writeable C-contiguous float64 "
+                             "array of B's shape")
+        X = X0
+    else:
+        X = np.zeros_like(B) if X0 is None else np.array(X0, np.float64, order="C", copy=True)
     A, keep = _csr(rp, ci, v)
     relres = np.zeros(m)
     res = L.CacgResult()

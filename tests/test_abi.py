@@ -107,3 +107,16 @@ def test_params_default_and_status_strings(lib):
     for code in (0, 1, -1, -2, -4, -5, -6, -7, -8):
         assert lib.cacg_status_string(code)
     assert lib.cacg_workspace_bytes(2097152, 16, 6, L.MIXED) > 3 * 2097152 * 96 * 4
+
+
+def test_overwrite_x0_argument_checks():
+    import numpy as np
+
+    import cacg_gb300 as cg
+
+    rp, ci, v = cg.gen_matrix("lap2d", 8)
+    B = np.ones((64, 2))
+    for X0 in (None, np.zeros((64, 2), np.float32), np.zeros((64, 3)),
+               np.zeros((2, 64)).T, np.zeros((64, 2))[:, :1]):
+        with pytest.raises(ValueError):
+            cg.solve(rp, ci, v, B, X0, overwrite_x0=True)

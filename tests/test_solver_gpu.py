@@ -107,6 +107,21 @@ def test_mixed_matches_fp64(lib):
     assert _rel(X32, X64) <= 1e-6
 
 
+def test_overwrite_x0_solves_in_place(lib):
+    rp, ci, v = cg.gen_matrix("st3d27", 20)
+    n = len(rp) - 1
+    B = cg.gen_rhs("uniform", n, 8, 3, -1.0, 1.0)
+    kw = dict(s=6, bounds=("given", 0.05, 52.0), tol=1e-8, maxit=300, rr_period=5,
+              precision="mixed")
+    X0 = np.full_like(B, 0.25)
+    Xc, ic = cg.solve(rp, ci, v, B, X0, **kw)
+    assert (X0 == 0.25).all()  # the copying path leaves X0 alone
+    Xi, ii = cg.solve(rp, ci, v, B, X0, overwrite_x0=True, **kw)
+    assert Xi is X0
+    assert ic["iterations"] == ii["iterations"]
+    assert np.array_equal(Xc, Xi)
+
+
 def test_mixed_lanczos_bounds_varcoef(lib):
     rp, ci, v = cg.gen_matrix("varcoef2d", 48, shift=1e-6, sigma=1.5, seed=3)
     n = len(rp) - 1
