@@ -19,7 +19,7 @@ BOUNDS_GERSCHGORIN, BOUNDS_GIVEN, BOUNDS_LANCZOS = 0, 1, 2
 TOL_ABS_COL0, TOL_REL_ALL = 0, 1
 FP64, MIXED = 0, 1
 GRAM_AUTO, GRAM_FMA, GRAM_DMMA, GRAM_TC, GRAM_TC_SLICES, GRAM_TC5 = 0, 1, 2, 3, 4, 5
-SPMM_AUTO, SPMM_CSR = 0, 1
+SPMM_AUTO, SPMM_CSR, SPMM_DIA_UNSTAGED = 0, 1, 2
 RESID_AUTO, RESID_FP64 = 0, 1
 VAL_F64, VAL_F32 = 0, 1
 

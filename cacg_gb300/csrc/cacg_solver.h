@@ -60,6 +60,14 @@ int launch_dia_spmm(cudaStream_t st, const DevMatrix *A, int w, const T *X, int6
                     int64_t ldy, const T *Z1, int64_t ldz1, const T *Z2, int64_t ldz2,
                     double ca, double cb, double cc);
 
+// The same product for FP32 blocks of 16k columns with the X rows of each
+// band of diagonals staged in shared memory by TMA (k_dia_ring.cu);
+// CACG_ERR_UNSUPPORTED when the operands or the diagonals do not fit its
+// layout.  *status gets kStatusTimeout if a bounded wait expires.
+int launch_dia_ring(cudaStream_t st, const DevMatrix *A, int w, const float *X, int64_t ldx,
+                    float *Y, int64_t ldy, const float *Z1, int64_t ldz1, const float *Z2,
+                    int64_t ldz2, double ca, double cb, double cc, int *status);
+
 // Device bytes of one solve's state (S, Q, AQ, R, small matrices, reduction
 // workspaces), the admission cost of a request.
 size_t solve_workspace_bytes(int64_t n, int m, int s, int prec, bool lanczos);

@@ -1,0 +1,378 @@
+// k_dia_ring.cu -- DIA SpMM (FP32, 16-column tiles) with the X rows staged in
+// shared memory by TMA: Y = ca A X + cb Z1 + cc Z2, the mixed mode's
+// Chebyshev basis step (src/common.c:182-256: Y = T_{j+1}, X = Z1 = T_j,
+// Z2 = T_{j-1}) and A Q (src/bcbcgKernel.c, the AQ product), A in the DIA
+// view of k_dia.cu.
+//
+// Bands.  The diagonals (ascending offsets) are cut into bands of nearby
+// offsets; the 27-point stencil on an N^3 grid gives three bands (dz = -1, 0,
+// +1), each 2N + 2 offsets wide.  A block of BR = 96 output rows starting at
+// r0 reads the X rows [r0 + lo_b, r0 + hi_b + BR) of band b.  A CTA walks an
+// item of consecutive blocks, so band b is a ring of K_b + 1 chunks of BR rows
+// in shared memory: K_b = ceil((hi_b - lo_b) / BR) + 1 chunks in use, one more
+// being loaded for the next block.  Each X row crosses L2 -> shared memory
+// once per band and item (plus the item's K_b - 1 start-up chunks), one 2-D
+// TMA load per chunk, and the FMAs read it from shared memory.  The block's
+// DIA values (ndiag x BR FP32) come by one more TMA load into a double buffer.
+//
+// Threads.  128 threads; thread (lr, c) = (tid / 4, tid % 4) computes rows
+// r0 + 3 lr + i (i < 3) of columns 4c .. 4c + 3.  Three rows per thread (an
+// odd count) puts the two rows that a quarter warp's 16-byte loads touch in
+// 64-byte slots of different parity, i.e. on disjoint banks.  Each output
+// sums its diagonals in ascending offset order with one FMA chain, as the
+// other DIA kernels and the CSR kernels do, so the results are bit-identical
+// to theirs.
+//
+// Items (sb consecutive blocks of one 16-column tile) go round-robin to the
+// CTAs, so at any time the CTAs work on neighbouring rows, and an X row that
+// the three bands read (N^2 rows apart) is an L2 hit after its first read.
+// The waits on the TMA barriers are bounded: on expiry the CTA sets
+// kStatusTimeout, waits (bounded) for the loads it has in flight and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "cacg_internal.cuh"
+#include "cacg_solver.h"
+#include "tc5_util.cuh"
+
+namespace cacg {
+
+namespace {
+
+constexpr int kRingThreads = 128;
+constexpr int kRingCpr = 4;                                // threads per row (float4 each)
+constexpr int kRingR = 3;                                  // rows per thread (odd)
+constexpr int kRingBR = kRingThreads / kRingCpr * kRingR;  // 96 rows per block
+constexpr int kRingCols = 16;                              // columns per tile
+constexpr int kRingRowBytes = kRingCols * 4;               // 64 bytes of a staged row
+constexpr int kRingBandMax = 4;
+constexpr int kRingItemsPerCta = 8;
+constexpr int kRingSmemMax = 227 * 1024;
+
+struct RingDesc {
+    int nb;                        // bands
+    int lo[kRingBandMax];          // lowest offset of band b
+    int K[kRingBandMax];           // chunks one block reads from band b
+    int cap[kRingBandMax];         // ring rows, (K + 1) * BR
+    int soff[kRingBandMax];        // byte offset of the ring in shared memory
+    int gfirst[kRingBandMax + 1];  // groups of band b: [gfirst[b], gfirst[b + 1])
+    int voff;                      // byte offset of the two value buffers
+    int vbytes;                    // bytes of one value buffer (ndiag x BR x 4, rounded up)
+    int vtx;                       // bytes one value load delivers (ndiag x BR x 4)
+    int boff;                      // byte offset of the two mbarriers
+    int z1band, z1rel;             // Z1 == X: band whose ring holds rows r0 .. r0+BR-1
+    int sb;                        // blocks per item
+    int tiles;                     // 16-column tiles
+};
+
+__device__ __forceinline__ void ring_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile(
+        "{\n"
+        ".reg .b64 st;\n"
+        "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n"
+        "}\n" ::"r"(t5_smem_u32(bar)),
+        "r"(bytes)
+        : "memory");
+}
+
+// 2-D tiled TMA load of the box at (x, y) (elements; x innermost) into dst
+__device__ __forceinline__ void ring_tma2d(void *dst, const CUtensorMap *map, int x, int y,
+                                           uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3}], [%4];\n" ::"r"(t5_smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(t5_smem_u32(bar))
+        : "memory");
+}
+
+// Loads of block t of an item (first: the K_b start-up chunks of every band)
+// and its values, completing on *bar.
+__device__ __forceinline__ void ring_issue(unsigned char *sm, const RingDesc &rd,
+                                           const CUtensorMap *tmx, const CUtensorMap *tmv,
+                                           int64_t R0, int col0, int t, bool first,
+                                           void *vdst, uint64_t *bar) {
+    unsigned bytes = (unsigned)rd.vtx;
+    for (int b = 0; b < rd.nb; ++b) bytes += (unsigned)((first ? rd.K[b] : 1) * kRingBR * kRingRowBytes);
+    ring_expect_tx(bar, bytes);
+    for (int b = 0; b < rd.nb; ++b) {
+        const int j0 = first ? 0 : t + rd.K[b] - 1, j1 = first ? rd.K[b] : j0 + 1;
+        for (int j = j0; j < j1; ++j) {
+            const int slot = j % (rd.K[b] + 1);
+            ring_tma2d(sm + rd.soff[b] + slot * (kRingBR * kRingRowBytes), tmx, col0,
+                       (int)(R0 + rd.lo[b] + (int64_t)j * kRingBR), bar);
+        }
+    }
+    ring_tma2d(vdst, tmv, (int)(R0 + (int64_t)t * kRingBR), 0, bar);
+}
+
+__global__ void __launch_bounds__(kRingThreads, 2)
+    dia_ring_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmv,
+                    int64_t n, int64_t nitems, const DiaDesc desc, const __grid_constant__ RingDesc rd,
+                    float *__restrict__ Y, int64_t ldy, const float *__restrict__ Z1, int64_t ldz1,
+                    const float *__restrict__ Z2, int64_t ldz2, float ca, float cb, float cc,
+                    int *__restrict__ status) {
+    extern __shared__ __align__(128) unsigned char ring_smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(ring_smem + rd.boff);
+    const int tid = threadIdx.x, lr = tid / kRingCpr, c = tid % kRingCpr;
+    const int rowoff = lr * kRingR;
+    if (tid == 0) {
+        t5_mbar_init(&bar[0], 1);
+        t5_mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        t5_fence_proxy_async();
+    }
+    __syncthreads();
+
+    const int64_t nblk = (n + kRingBR - 1) / kRingBR;
+    unsigned u = 0;       // blocks this CTA has computed (barrier stage and parity)
+    unsigned issued = 0;  // blocks whose loads are issued (thread 0)
+    bool timeout = false;
+    for (int64_t it = blockIdx.x; it < nitems && !timeout; it += gridDim.x) {
+        const int64_t ri = it / rd.tiles;
+        const int col0 = (int)(it % rd.tiles) * kRingCols;
+        const int64_t b0 = ri * rd.sb;
+        const int nbk = (int)std::min<int64_t>(rd.sb, nblk - b0);
+        const int64_t R0 = b0 * kRingBR;
+        if (tid == 0) {
+            // the previous item's blocks are done (barrier at the end of each block)
+            t5_fence_proxy_async();
+            ring_issue(ring_smem, rd, &tmx, &tmv, R0, col0, 0, true,
+                       ring_smem + rd.voff + (u & 1) * rd.vbytes, &bar[u & 1]);
+            ++issued;
+            if (nbk > 1) {
+                ring_issue(ring_smem, rd, &tmx, &tmv, R0, col0, 1, false,
+                           ring_smem + rd.voff + ((u + 1) & 1) * rd.vbytes, &bar[(u + 1) & 1]);
+                ++issued;
+            }
+        }
+        for (int t = 0; t < nbk; ++t, ++u) {
+            if (tid == 0 && t >= 1 && t + 1 < nbk) {
+                // block t + 1 takes the slot of block t - 1's first chunk and the
+                // value buffer of block t - 1, both released by the last barrier
+                t5_fence_proxy_async();
+                ring_issue(ring_smem, rd, &tmx, &tmv, R0, col0, t + 1, false,
+                           ring_smem + rd.voff + ((u + 1) & 1) * rd.vbytes, &bar[(u + 1) & 1]);
+                ++issued;
+            }
+            const bool ok = t5_mbar_wait(&bar[u & 1], (u >> 1) & 1);
+            if (__syncthreads_or(!ok)) {
+                timeout = true;
+                break;
+            }
+            const float *vb = reinterpret_cast<const float *>(ring_smem + rd.voff + (u & 1) * rd.vbytes);
+            float4 acc[kRingR];
+#pragma unroll
+            for (int i = 0; i < kRingR; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int b = 0; b < rd.nb; ++b) {
+                const unsigned char *ring = ring_smem + rd.soff[b] + c * 16;
+                const int cap = rd.cap[b];
+                const int base = (int)(((int64_t)t * kRingBR) % cap);
+                for (int g = rd.gfirst[b]; g < rd.gfirst[b + 1]; ++g) {
+                    const int d0 = desc.gstart[g], G = desc.gstart[g + 1] - d0;
+                    int q = base + rowoff + (int)(desc.off[d0] - rd.lo[b]);
+                    if (q >= cap) q -= cap;
+                    float4 win[kRingR + kDiaGroupMax - 1];
+#pragma unroll
+                    for (int w = 0; w < kRingR + kDiaGroupMax - 1; ++w) {
+                        if (w < kRingR + G - 1) {
+                            int qq = q + w;
+                            if (qq >= cap) qq -= cap;
+                            win[w] = *reinterpret_cast<const float4 *>(ring + qq * kRingRowBytes);
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < kDiaGroupMax; ++j) {
+                        if (j < G) {
+                            const float *vp = vb + (d0 + j) * kRingBR + rowoff;
+#pragma unroll
+                            for (int i = 0; i < kRingR; ++i) {
+                                const float v = vp[i];
+                                acc[i].x = fmaf(v, win[i + j].x, acc[i].x);
+                                acc[i].y = fmaf(v, win[i + j].y, acc[i].y);
+                                acc[i].z = fmaf(v, win[i + j].z, acc[i].z);
+                                acc[i].w = fmaf(v, win[i + j].w, acc[i].w);
+                            }
+                        }
+                    }
+                }
+            }
+            const int64_t rbase = R0 + (int64_t)t * kRingBR + rowoff;
+            const int col = col0 + 4 * c;
+            int zq = 0, zcap = 0;
+            if (rd.z1band >= 0) {
+                zcap = rd.cap[rd.z1band];
+                zq = (int)(((int64_t)t * kRingBR) % zcap) + rowoff + rd.z1rel;
+                if (zq >= zcap) zq -= zcap;
+            }
+#pragma unroll
+            for (int i = 0; i < kRingR; ++i) {
+                const int64_t row = rbase + i;
+                if (row >= n) break;
+                float4 y = make_float4(ca * acc[i].x, ca * acc[i].y, ca * acc[i].z, ca * acc[i].w);
+                if (Z1) {
+                    float4 z;
+                    if (rd.z1band >= 0) {
+                        int qq = zq + i;
+                        if (qq >= zcap) qq -= zcap;
+                        z = *reinterpret_cast<const float4 *>(ring_smem + rd.soff[rd.z1band] +
+                                                              c * 16 + qq * kRingRowBytes);
+                    } else {
+                        z = *reinterpret_cast<const float4 *>(Z1 + row * ldz1 + col);
+                    }
+                    y.x = fmaf(cb, z.x, y.x);
+                    y.y = fmaf(cb, z.y, y.y);
+                    y.z = fmaf(cb, z.z, y.z);
+                    y.w = fmaf(cb, z.w, y.w);
+                }
+                if (Z2) {
+                    const float4 z = *reinterpret_cast<const float4 *>(Z2 + row * ldz2 + col);
+                    y.x = fmaf(cc, z.x, y.x);
+                    y.y = fmaf(cc, z.y, y.y);
+                    y.z = fmaf(cc, z.z, y.z);
+                    y.w = fmaf(cc, z.w, y.w);
+                }
+                *reinterpret_cast<float4 *>(Y + row * ldy + col) = y;
+            }
+            __syncthreads();  // ring slot of this block's first chunk and its values are free
+        }
+    }
+    if (timeout && tid == 0) {
+        atomicOr(status, kStatusTimeout);
+        // let the loads in flight land before the CTA's shared memory goes away
+        for (unsigned v = u; v < issued; ++v) t5_mbar_wait(&bar[v & 1], (v >> 1) & 1);
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// FP32 2-D map: `inner` elements per row (contiguous), `outer` rows
+// `row_bytes` apart; box box_in x box_out; zero fill outside.
+bool encode_2d(CUtensorMap *m, const void *base, uint64_t inner, uint64_t outer,
+               uint64_t row_bytes, uint32_t box_in, uint32_t box_out,
+               CUtensorMapL2promotion promo) {
+    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {row_bytes};
+    cuuint32_t box[2] = {box_in, box_out};
+    cuuint32_t es[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims, strides, box,
+              es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, promo,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Bands, rings and shared-memory layout for the matrix's diagonals; false
+// when they do not fit.
+bool ring_plan(const DiaDesc &D, RingDesc *rd, size_t *smem) {
+    std::vector<int> gfirst;
+    std::vector<int64_t> lo, hi;
+    for (int g = 0; g < D.ngroups; ++g) {
+        const int64_t a = D.off[D.gstart[g]], e = D.off[D.gstart[g + 1] - 1];
+        if (!lo.empty() && a - hi.back() < 2 * kRingBR) {
+            hi.back() = e;  // a gap this small costs less than a ring of its own
+            continue;
+        }
+        gfirst.push_back(g);
+        lo.push_back(a);
+        hi.push_back(e);
+    }
+    const int nb = (int)lo.size();
+    if (nb == 0 || nb > kRingBandMax) return false;
+    *rd = RingDesc{};
+    rd->nb = nb;
+    rd->z1band = -1;
+    size_t off = 0;
+    for (int b = 0; b < nb; ++b) {
+        const int64_t span = hi[b] - lo[b];
+        rd->lo[b] = (int)lo[b];
+        rd->K[b] = (int)((span + kRingBR - 1) / kRingBR) + 1;
+        rd->cap[b] = (rd->K[b] + 1) * kRingBR;
+        rd->soff[b] = (int)off;
+        rd->gfirst[b] = gfirst[b];
+        off += (size_t)rd->cap[b] * kRingRowBytes;
+        if (lo[b] <= 0 && hi[b] >= 0) {
+            rd->z1band = b;
+            rd->z1rel = (int)-lo[b];
+        }
+    }
+    rd->gfirst[nb] = D.ngroups;
+    rd->voff = (int)off;
+    rd->vtx = D.ndiag * kRingBR * 4;
+    rd->vbytes = (rd->vtx + 127) / 128 * 128;
+    off += 2 * (size_t)rd->vbytes;
+    rd->boff = (int)off;
+    off += 16;
+    *smem = off;
+    return off <= (size_t)kRingSmemMax;
+}
+
+}  // namespace
+
+int launch_dia_ring(cudaStream_t st, const DevMatrix *A, int w, const float *X, int64_t ldx,
+                    float *Y, int64_t ldy, const float *Z1, int64_t ldz1, const float *Z2,
+                    int64_t ldz2, double ca, double cb, double cc, int *status) {
+    if (!A || !A->dia32 || A->dia_ndiag <= 0 || !status) return CACG_ERR_UNSUPPORTED;
+    const int64_t n = A->n;
+    if (n <= 0 || n >= (1ll << 30) || w <= 0 || w % kRingCols != 0) return CACG_ERR_UNSUPPORTED;
+    if (!aligned16(X) || !aligned16(Y) || ldx % 4 || ldy % 4 || ldx < w || ldy < w)
+        return CACG_ERR_UNSUPPORTED;
+    if (Z1 && (!aligned16(Z1) || ldz1 % 4)) return CACG_ERR_UNSUPPORTED;
+    if (Z2 && (!aligned16(Z2) || ldz2 % 4)) return CACG_ERR_UNSUPPORTED;
+    if (A->dia_npad % 4 || !aligned16(A->dia32)) return CACG_ERR_UNSUPPORTED;
+    RingDesc rd;
+    size_t smem = 0;
+    if (!ring_plan(A->dia, &rd, &smem)) return CACG_ERR_UNSUPPORTED;
+    if (!(Z1 == X && ldz1 == ldx)) rd.z1band = -1;  // Z1 read from global memory
+    CUtensorMap tmx, tmv;
+    if (!encode_2d(&tmx, X, (uint64_t)w, (uint64_t)n, (uint64_t)ldx * 4, kRingCols, kRingBR,
+                   CU_TENSOR_MAP_L2_PROMOTION_NONE) ||
+        !encode_2d(&tmv, A->dia32, (uint64_t)A->dia_npad, (uint64_t)A->dia_ndiag,
+                   (uint64_t)A->dia_npad * 4, kRingBR, (uint32_t)A->dia_ndiag,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B))
+        return CACG_ERR_UNSUPPORTED;
+    static const int per_sm = [] {
+        cudaFuncSetAttribute(dia_ring_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kRingSmemMax);
+        return 0;
+    }();
+    (void)per_sm;
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dia_ring_kernel, kRingThreads, smem) !=
+            cudaSuccess ||
+        occ < 1) {
+        cudaGetLastError();
+        return CACG_ERR_UNSUPPORTED;
+    }
+    rd.tiles = w / kRingCols;
+    const int64_t grid0 = (int64_t)sm_count() * std::min(occ, 2);
+    const int64_t nblk = (n + kRingBR - 1) / kRingBR;
+    int kmax = 1;
+    for (int b = 0; b < rd.nb; ++b) kmax = std::max(kmax, rd.K[b]);
+    // about kRingItemsPerCta items per CTA; an item at least 2 K blocks long
+    const int64_t want = std::max<int64_t>(1, grid0 * kRingItemsPerCta / rd.tiles);
+    rd.sb = (int)std::max<int64_t>(2 * kmax, (nblk + want - 1) / want);
+    const int64_t nitems = (nblk + rd.sb - 1) / rd.sb * rd.tiles;
+    const int64_t grid = std::min<int64_t>(grid0, nitems);
+    dia_ring_kernel<<<(unsigned)grid, kRingThreads, smem, st>>>(
+        tmx, tmv, n, nitems, A->dia, rd, Y, ldy, Z1, ldz1, Z2, ldz2, (float)ca, (float)cb,
+        (float)cc, status);
+    return check_launch();
+}
+
+}  // namespace cacg

@@ -536,6 +536,13 @@ struct Solver {
     int spmm(const T *X, int64_t ldx, T *Y, int64_t ldy, int w, const T *Z1, int64_t ldz1,
              const T *Z2, int64_t ldz2, double ca, double cb, double cc) {
         if (uses_dia()) {
+            if constexpr (std::is_same<T, float>::value) {
+                if (p.spmm_format == CACG_SPMM_AUTO) {
+                    int rc = launch_dia_ring(st, A, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb,
+                                             cc, b.status);
+                    if (rc != CACG_ERR_UNSUPPORTED) return rc;
+                }
+            }
             int rc = launch_dia_spmm<T>(st, A, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc);
             if (rc != CACG_ERR_UNSUPPORTED) return rc;
         }

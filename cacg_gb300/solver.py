@@ -64,6 +64,7 @@ class Params:
     stream: int = 0
     exact_updates: bool = False     # mixed: float-float X/R update products
     spmm_format: str = "auto"       # "auto" (DIA view when the matrix has one) | "csr"
+                                    # | "dia_unstaged" (DIA without shared-memory staging)
     residual: str = "auto"          # mixed: "auto" (float-float replacements on DIA) | "fp64"
     use_graph: bool = False         # replay captured outer iterations (non-default stream)
 
@@ -91,7 +92,8 @@ class Params:
         p.lanczos_seed = self.lanczos_seed
         p.stream = self.stream or None
         p.exact_updates = 1 if self.exact_updates else 0
-        p.spmm_format = {"auto": L.SPMM_AUTO, "csr": L.SPMM_CSR}[self.spmm_format]
+        p.spmm_format = {"auto": L.SPMM_AUTO, "csr": L.SPMM_CSR,
+                         "dia_unstaged": L.SPMM_DIA_UNSTAGED}[self.spmm_format]
         p.residual_precision = {"auto": L.RESID_AUTO, "fp64": L.RESID_FP64}[self.residual]
         p.use_graph = 1 if self.use_graph else 0
         return p

@@ -68,6 +68,8 @@ extern "C" {
 
 #define CACG_SPMM_AUTO 0
 #define CACG_SPMM_CSR 1 /* always the CSR kernels */
+#define CACG_SPMM_DIA_UNSTAGED 2 /* the DIA view, read through the caches only (no
+                                    shared-memory staging of X); results identical */
 
 #define CACG_RESID_AUTO 0
 #define CACG_RESID_FP64 1 /* residual replacements in FP64 as well */
@@ -122,7 +124,9 @@ typedef struct cacg_params {
     int32_t exact_updates; /* MIXED: X/R update products summed in float-float
                               instead of FP32 FMAs */
     int32_t spmm_format;  /* CACG_SPMM_*: AUTO uses the matrix's DIA view when it
-                             has one (results bit-identical to CSR) */
+                             has one (results bit-identical to CSR); MIXED with
+                             16-column blocks stages the X rows of each band of
+                             diagonals in shared memory (TMA) */
     int32_t residual_precision; /* CACG_RESID_*: MIXED with a DIA view computes the
                                    periodic residual replacements in float-float
                                    (about 44 bits, FP32 pipe) unless FP64 is asked

@@ -48,6 +48,32 @@ def test_dia_solve_bit_identical_to_csr(lib, kind, N, ndiag, m, s, prec):
         assert np.array_equal(Xd, Xc)
 
 
+@pytest.mark.parametrize("kind,N,m,s", [("st3d27", 40, 16, 6), ("st3d27", 26, 32, 3),
+                                        ("lap3d7", 48, 16, 4), ("lap2d", 300, 16, 4),
+                                        ("st3d27", 20, 20, 4), ("st3d27", 12, 16, 6)])
+def test_staged_dia_bit_identical(lib, kind, N, m, s):
+    """MIXED, 16k-column blocks: the shared-memory staged DIA SpMM (bands of
+    diagonals in TMA-fed rings; three bands for the 3-D grids and the 300^2
+    grid, one for 12^3) against the unstaged DIA kernel and CSR; m = 20 is
+    not a multiple of 16 and takes the unstaged kernel."""
+    rp, ci, v = cg.gen_matrix(kind, N, shift=1e-3, sigma=1.0, seed=5)
+    n = len(rp) - 1
+    B = cg.gen_rhs("normal", n, m, 7)
+    M = cg.Matrix(rp, ci, v, want_fp32=True)
+    kw = dict(s=s, bounds="gerschgorin", tol=1e-8, maxit=600, precision="mixed",
+              residual="fp64")
+    out = {f: _solve_dev(M, B, cg.Params(spmm_format=f, **kw))
+           for f in ("auto", "dia_unstaged", "csr")}
+    M.close()
+    Xa, ia = out["auto"]
+    for f in ("dia_unstaged", "csr"):
+        X, i = out[f]
+        assert i["status"] == 0 and ia["status"] == 0
+        assert i["iterations"] == ia["iterations"], f
+        assert np.array_equal(X, Xa), f
+    assert ia["true_relres_max"] <= 1e-8
+
+
 def test_dia_not_built_for_irregular_matrix(lib):
     rng = np.random.default_rng(3)
     n = 2000
