@@ -66,6 +66,8 @@ struct RingDesc {
     int z1band, z1rel;             // Z1 == X: band whose ring holds rows r0 .. r0+BR-1
     int sb;                        // blocks per item
     int tiles;                     // 16-column tiles
+    int grel[kDiaMax];             // group g: first offset - lo of its band
+    int gdg[kDiaMax];              // group g: first diagonal | diagonals << 8
 };
 
 __device__ __forceinline__ void ring_expect_tx(uint64_t *bar, unsigned bytes) {
@@ -108,6 +110,41 @@ __device__ __forceinline__ void ring_issue(unsigned char *sm, const RingDesc &rd
     ring_tma2d(vdst, tmv, (int)(R0 + (int64_t)t * kRingBR), 0, bar);
 }
 
+// One group of G adjacent diagonals: the window of R + G - 1 staged rows
+// starting at ring row q (wrapping at cap), G x R values from vp (stride BR
+// per diagonal), FMAs into acc in diagonal order.
+template <int G>
+__device__ __forceinline__ void ring_group(const unsigned char *ring, int q, int cap,
+                                           const float *vp, float4 (&acc)[kRingR]) {
+    constexpr int W = kRingR + G - 1;
+    float4 win[W];
+    const int lim = cap - q;  // rows before the ring wraps
+    if (lim >= W) {
+        const unsigned char *p = ring + q * kRingRowBytes;
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+            win[w] = *reinterpret_cast<const float4 *>(p + w * kRingRowBytes);
+    } else {
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+            win[w] = *reinterpret_cast<const float4 *>(
+                ring + (q + w - (w >= lim ? cap : 0)) * kRingRowBytes);
+    }
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+        float v[kRingR];
+#pragma unroll
+        for (int i = 0; i < kRingR; ++i) v[i] = vp[j * kRingBR + i];
+#pragma unroll
+        for (int i = 0; i < kRingR; ++i) {
+            acc[i].x = fmaf(v[i], win[i + j].x, acc[i].x);
+            acc[i].y = fmaf(v[i], win[i + j].y, acc[i].y);
+            acc[i].z = fmaf(v[i], win[i + j].z, acc[i].z);
+            acc[i].w = fmaf(v[i], win[i + j].w, acc[i].w);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kRingThreads, 2)
     dia_ring_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmv,
                     int64_t n, int64_t nitems, const DiaDesc desc, const __grid_constant__ RingDesc rd,
@@ -136,6 +173,9 @@ __global__ void __launch_bounds__(kRingThreads, 2)
         const int64_t b0 = ri * rd.sb;
         const int nbk = (int)std::min<int64_t>(rd.sb, nblk - b0);
         const int64_t R0 = b0 * kRingBR;
+        int base[kRingBandMax];  // ring row of the block's first row, band b: t BR mod cap
+#pragma unroll
+        for (int b = 0; b < kRingBandMax; ++b) base[b] = 0;
         if (tid == 0) {
             // the previous item's blocks are done (barrier at the end of each block)
             t5_fence_proxy_async();
@@ -162,65 +202,55 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                 timeout = true;
                 break;
             }
-            const float *vb = reinterpret_cast<const float *>(ring_smem + rd.voff + (u & 1) * rd.vbytes);
+            const float *vb =
+                reinterpret_cast<const float *>(ring_smem + rd.voff + (u & 1) * rd.vbytes) + rowoff;
             float4 acc[kRingR];
 #pragma unroll
             for (int i = 0; i < kRingR; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int b = 0; b < rd.nb; ++b) {
-                const unsigned char *ring = ring_smem + rd.soff[b] + c * 16;
-                const int cap = rd.cap[b];
-                const int base = (int)(((int64_t)t * kRingBR) % cap);
-                for (int g = rd.gfirst[b]; g < rd.gfirst[b + 1]; ++g) {
-                    const int d0 = desc.gstart[g], G = desc.gstart[g + 1] - d0;
-                    int q = base + rowoff + (int)(desc.off[d0] - rd.lo[b]);
-                    if (q >= cap) q -= cap;
-                    float4 win[kRingR + kDiaGroupMax - 1];
+            int zq = -1;  // ring row of the thread's first row in the Z1 band
 #pragma unroll
-                    for (int w = 0; w < kRingR + kDiaGroupMax - 1; ++w) {
-                        if (w < kRingR + G - 1) {
-                            int qq = q + w;
-                            if (qq >= cap) qq -= cap;
-                            win[w] = *reinterpret_cast<const float4 *>(ring + qq * kRingRowBytes);
-                        }
+            for (int b = 0; b < kRingBandMax; ++b) {
+                if (b < rd.nb) {
+                    const unsigned char *ring = ring_smem + rd.soff[b] + c * 16;
+                    const int cap = rd.cap[b];
+                    const int qb = base[b] + rowoff;
+                    if (b == rd.z1band) {
+                        zq = qb + rd.z1rel;
+                        if (zq >= cap) zq -= cap;
                     }
-#pragma unroll
-                    for (int j = 0; j < kDiaGroupMax; ++j) {
-                        if (j < G) {
-                            const float *vp = vb + (d0 + j) * kRingBR + rowoff;
-#pragma unroll
-                            for (int i = 0; i < kRingR; ++i) {
-                                const float v = vp[i];
-                                acc[i].x = fmaf(v, win[i + j].x, acc[i].x);
-                                acc[i].y = fmaf(v, win[i + j].y, acc[i].y);
-                                acc[i].z = fmaf(v, win[i + j].z, acc[i].z);
-                                acc[i].w = fmaf(v, win[i + j].w, acc[i].w);
-                            }
+                    for (int g = rd.gfirst[b]; g < rd.gfirst[b + 1]; ++g) {
+                        int q = qb + rd.grel[g];
+                        if (q >= cap) q -= cap;
+                        const int dg = rd.gdg[g];
+                        const float *vp = vb + (dg & 0xFF) * kRingBR;
+                        switch (dg >> 8) {
+                            case 1: ring_group<1>(ring, q, cap, vp, acc); break;
+                            case 2: ring_group<2>(ring, q, cap, vp, acc); break;
+                            case 3: ring_group<3>(ring, q, cap, vp, acc); break;
+                            default: ring_group<4>(ring, q, cap, vp, acc); break;
                         }
                     }
                 }
             }
             const int64_t rbase = R0 + (int64_t)t * kRingBR + rowoff;
             const int col = col0 + 4 * c;
-            int zq = 0, zcap = 0;
-            if (rd.z1band >= 0) {
-                zcap = rd.cap[rd.z1band];
-                zq = (int)(((int64_t)t * kRingBR) % zcap) + rowoff + rd.z1rel;
-                if (zq >= zcap) zq -= zcap;
-            }
+            float *yp = Y + rbase * ldy + col;
+            const float *z1p = Z1 ? Z1 + rbase * ldz1 + col : nullptr;
+            const float *z2p = Z2 ? Z2 + rbase * ldz2 + col : nullptr;
 #pragma unroll
             for (int i = 0; i < kRingR; ++i) {
-                const int64_t row = rbase + i;
-                if (row >= n) break;
+                if (rbase + i >= n) break;
                 float4 y = make_float4(ca * acc[i].x, ca * acc[i].y, ca * acc[i].z, ca * acc[i].w);
                 if (Z1) {
                     float4 z;
-                    if (rd.z1band >= 0) {
+                    if (zq >= 0) {
+                        const int zcap = rd.cap[rd.z1band];
                         int qq = zq + i;
                         if (qq >= zcap) qq -= zcap;
                         z = *reinterpret_cast<const float4 *>(ring_smem + rd.soff[rd.z1band] +
                                                               c * 16 + qq * kRingRowBytes);
                     } else {
-                        z = *reinterpret_cast<const float4 *>(Z1 + row * ldz1 + col);
+                        z = *reinterpret_cast<const float4 *>(z1p + i * ldz1);
                     }
                     y.x = fmaf(cb, z.x, y.x);
                     y.y = fmaf(cb, z.y, y.y);
@@ -228,13 +258,20 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                     y.w = fmaf(cb, z.w, y.w);
                 }
                 if (Z2) {
-                    const float4 z = *reinterpret_cast<const float4 *>(Z2 + row * ldz2 + col);
+                    const float4 z = *reinterpret_cast<const float4 *>(z2p + i * ldz2);
                     y.x = fmaf(cc, z.x, y.x);
                     y.y = fmaf(cc, z.y, y.y);
                     y.z = fmaf(cc, z.z, y.z);
                     y.w = fmaf(cc, z.w, y.w);
                 }
-                *reinterpret_cast<float4 *>(Y + row * ldy + col) = y;
+                *reinterpret_cast<float4 *>(yp + i * ldy) = y;
+            }
+#pragma unroll
+            for (int b = 0; b < kRingBandMax; ++b) {
+                if (b < rd.nb) {
+                    base[b] += kRingBR;
+                    if (base[b] >= rd.cap[b]) base[b] -= rd.cap[b];
+                }
             }
             __syncthreads();  // ring slot of this block's first chunk and its values are free
         }
@@ -312,6 +349,11 @@ bool ring_plan(const DiaDesc &D, RingDesc *rd, size_t *smem) {
         }
     }
     rd->gfirst[nb] = D.ngroups;
+    for (int b = 0; b < nb; ++b)
+        for (int g = rd->gfirst[b]; g < rd->gfirst[b + 1]; ++g) {
+            rd->grel[g] = (int)(D.off[D.gstart[g]] - lo[b]);
+            rd->gdg[g] = D.gstart[g] | ((D.gstart[g + 1] - D.gstart[g]) << 8);
+        }
     rd->voff = (int)off;
     rd->vtx = D.ndiag * kRingBR * 4;
     rd->vbytes = (rd->vtx + 127) / 128 * 128;
