@@ -49,6 +49,7 @@ constexpr int kRingBR = kRingThreads / kRingCpr * kRingR;  // 96 rows per block
 constexpr int kRingCols = 16;                              // columns per tile
 constexpr int kRingRowBytes = kRingCols * 4;               // 64 bytes of a staged row
 constexpr int kRingBandMax = 4;
+constexpr int kRingMirror = 8;  // rows of slot 0 repeated after a ring's end
 constexpr int kRingItemsPerCta = 8;
 constexpr int kRingSmemMax = 227 * 1024;
 
@@ -56,7 +57,7 @@ struct RingDesc {
     int nb;                        // bands
     int lo[kRingBandMax];          // lowest offset of band b
     int K[kRingBandMax];           // chunks one block reads from band b
-    int cap[kRingBandMax];         // ring rows, (K + 1) * BR
+    int cap[kRingBandMax];         // ring rows, (K + 1) * BR (plus kRingMirror rows)
     int soff[kRingBandMax];        // byte offset of the ring in shared memory
     int gfirst[kRingBandMax + 1];  // groups of band b: [gfirst[b], gfirst[b + 1])
     int voff;                      // byte offset of the two value buffers
@@ -91,45 +92,47 @@ __device__ __forceinline__ void ring_tma2d(void *dst, const CUtensorMap *map, in
 }
 
 // Loads of block t of an item (first: the K_b start-up chunks of every band)
-// and its values, completing on *bar.
+// and its values, completing on *bar.  A chunk that goes to slot 0 also
+// fills the ring's mirror rows (its first kRingMirror rows, after the last
+// slot), so a window of consecutive ring rows never wraps.
 __device__ __forceinline__ void ring_issue(unsigned char *sm, const RingDesc &rd,
-                                           const CUtensorMap *tmx, const CUtensorMap *tmv,
-                                           int64_t R0, int col0, int t, bool first,
-                                           void *vdst, uint64_t *bar) {
+                                           const CUtensorMap *tmx, const CUtensorMap *tmm,
+                                           const CUtensorMap *tmv, int64_t R0, int col0, int t,
+                                           bool first, void *vdst, uint64_t *bar) {
     unsigned bytes = (unsigned)rd.vtx;
-    for (int b = 0; b < rd.nb; ++b) bytes += (unsigned)((first ? rd.K[b] : 1) * kRingBR * kRingRowBytes);
+    for (int b = 0; b < rd.nb; ++b) {
+        const int j0 = first ? 0 : t + rd.K[b] - 1, j1 = first ? rd.K[b] : j0 + 1;
+        for (int j = j0; j < j1; ++j)
+            bytes += kRingBR * kRingRowBytes +
+                     (j % (rd.K[b] + 1) == 0 ? kRingMirror * kRingRowBytes : 0);
+    }
     ring_expect_tx(bar, bytes);
     for (int b = 0; b < rd.nb; ++b) {
         const int j0 = first ? 0 : t + rd.K[b] - 1, j1 = first ? rd.K[b] : j0 + 1;
         for (int j = j0; j < j1; ++j) {
             const int slot = j % (rd.K[b] + 1);
-            ring_tma2d(sm + rd.soff[b] + slot * (kRingBR * kRingRowBytes), tmx, col0,
-                       (int)(R0 + rd.lo[b] + (int64_t)j * kRingBR), bar);
+            const int y = (int)(R0 + rd.lo[b] + (int64_t)j * kRingBR);
+            ring_tma2d(sm + rd.soff[b] + slot * (kRingBR * kRingRowBytes), tmx, col0, y, bar);
+            if (slot == 0)
+                ring_tma2d(sm + rd.soff[b] + rd.cap[b] * kRingRowBytes, tmm, col0, y, bar);
         }
     }
     ring_tma2d(vdst, tmv, (int)(R0 + (int64_t)t * kRingBR), 0, bar);
 }
 
 // One group of G adjacent diagonals: the window of R + G - 1 staged rows
-// starting at ring row q (wrapping at cap), G x R values from vp (stride BR
-// per diagonal), FMAs into acc in diagonal order.
+// starting at ring row q < cap (the mirror rows continue the ring past cap),
+// G x R values from vp (stride BR per diagonal), FMAs into acc in diagonal
+// order.
 template <int G>
-__device__ __forceinline__ void ring_group(const unsigned char *ring, int q, int cap,
-                                           const float *vp, float4 (&acc)[kRingR]) {
+__device__ __forceinline__ void ring_group(const unsigned char *ring, int q, const float *vp,
+                                           float4 (&acc)[kRingR]) {
     constexpr int W = kRingR + G - 1;
+    static_assert(W - 1 <= kRingMirror, "window longer than the mirror");
     float4 win[W];
-    const int lim = cap - q;  // rows before the ring wraps
-    if (lim >= W) {
-        const unsigned char *p = ring + q * kRingRowBytes;
+    const unsigned char *p = ring + q * kRingRowBytes;
 #pragma unroll
-        for (int w = 0; w < W; ++w)
-            win[w] = *reinterpret_cast<const float4 *>(p + w * kRingRowBytes);
-    } else {
-#pragma unroll
-        for (int w = 0; w < W; ++w)
-            win[w] = *reinterpret_cast<const float4 *>(
-                ring + (q + w - (w >= lim ? cap : 0)) * kRingRowBytes);
-    }
+    for (int w = 0; w < W; ++w) win[w] = *reinterpret_cast<const float4 *>(p + w * kRingRowBytes);
 #pragma unroll
     for (int j = 0; j < G; ++j) {
         float v[kRingR];
@@ -145,8 +148,13 @@ __device__ __forceinline__ void ring_group(const unsigned char *ring, int q, int
     }
 }
 
+// NB > 0: NB bands of GPB groups of G diagonals each (the 27-point stencil's
+// 3 x 3 x 3), loops unrolled so the window loads of later groups can be
+// issued ahead of earlier groups' FMAs; NB = 0: any layout, read from rd.
+template <int NB, int GPB, int G>
 __global__ void __launch_bounds__(kRingThreads, 2)
-    dia_ring_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmv,
+    dia_ring_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmm,
+                    const __grid_constant__ CUtensorMap tmv,
                     int64_t n, int64_t nitems, const DiaDesc desc, const __grid_constant__ RingDesc rd,
                     float *__restrict__ Y, int64_t ldy, const float *__restrict__ Z1, int64_t ldz1,
                     const float *__restrict__ Z2, int64_t ldz2, float ca, float cb, float cc,
@@ -179,11 +187,11 @@ __global__ void __launch_bounds__(kRingThreads, 2)
         if (tid == 0) {
             // the previous item's blocks are done (barrier at the end of each block)
             t5_fence_proxy_async();
-            ring_issue(ring_smem, rd, &tmx, &tmv, R0, col0, 0, true,
+            ring_issue(ring_smem, rd, &tmx, &tmm, &tmv, R0, col0, 0, true,
                        ring_smem + rd.voff + (u & 1) * rd.vbytes, &bar[u & 1]);
             ++issued;
             if (nbk > 1) {
-                ring_issue(ring_smem, rd, &tmx, &tmv, R0, col0, 1, false,
+                ring_issue(ring_smem, rd, &tmx, &tmm, &tmv, R0, col0, 1, false,
                            ring_smem + rd.voff + ((u + 1) & 1) * rd.vbytes, &bar[(u + 1) & 1]);
                 ++issued;
             }
@@ -193,7 +201,7 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                 // block t + 1 takes the slot of block t - 1's first chunk and the
                 // value buffer of block t - 1, both released by the last barrier
                 t5_fence_proxy_async();
-                ring_issue(ring_smem, rd, &tmx, &tmv, R0, col0, t + 1, false,
+                ring_issue(ring_smem, rd, &tmx, &tmm, &tmv, R0, col0, t + 1, false,
                            ring_smem + rd.voff + ((u + 1) & 1) * rd.vbytes, &bar[(u + 1) & 1]);
                 ++issued;
             }
@@ -209,8 +217,8 @@ __global__ void __launch_bounds__(kRingThreads, 2)
             for (int i = 0; i < kRingR; ++i) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
             int zq = -1;  // ring row of the thread's first row in the Z1 band
 #pragma unroll
-            for (int b = 0; b < kRingBandMax; ++b) {
-                if (b < rd.nb) {
+            for (int b = 0; b < (NB > 0 ? NB : kRingBandMax); ++b) {
+                if (NB > 0 || b < rd.nb) {
                     const unsigned char *ring = ring_smem + rd.soff[b] + c * 16;
                     const int cap = rd.cap[b];
                     const int qb = base[b] + rowoff;
@@ -218,16 +226,26 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                         zq = qb + rd.z1rel;
                         if (zq >= cap) zq -= cap;
                     }
-                    for (int g = rd.gfirst[b]; g < rd.gfirst[b + 1]; ++g) {
-                        int q = qb + rd.grel[g];
-                        if (q >= cap) q -= cap;
-                        const int dg = rd.gdg[g];
-                        const float *vp = vb + (dg & 0xFF) * kRingBR;
-                        switch (dg >> 8) {
-                            case 1: ring_group<1>(ring, q, cap, vp, acc); break;
-                            case 2: ring_group<2>(ring, q, cap, vp, acc); break;
-                            case 3: ring_group<3>(ring, q, cap, vp, acc); break;
-                            default: ring_group<4>(ring, q, cap, vp, acc); break;
+                    if constexpr (NB > 0) {
+#pragma unroll
+                        for (int gg = 0; gg < GPB; ++gg) {
+                            const int g = b * GPB + gg;
+                            int q = qb + rd.grel[g];
+                            if (q >= cap) q -= cap;
+                            ring_group<G>(ring, q, vb + (rd.gdg[g] & 0xFF) * kRingBR, acc);
+                        }
+                    } else {
+                        for (int g = rd.gfirst[b]; g < rd.gfirst[b + 1]; ++g) {
+                            int q = qb + rd.grel[g];
+                            if (q >= cap) q -= cap;
+                            const int dg = rd.gdg[g];
+                            const float *vp = vb + (dg & 0xFF) * kRingBR;
+                            switch (dg >> 8) {
+                                case 1: ring_group<1>(ring, q, vp, acc); break;
+                                case 2: ring_group<2>(ring, q, vp, acc); break;
+                                case 3: ring_group<3>(ring, q, vp, acc); break;
+                                default: ring_group<4>(ring, q, vp, acc); break;
+                            }
                         }
                     }
                 }
@@ -244,11 +262,8 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                 if (Z1) {
                     float4 z;
                     if (zq >= 0) {
-                        const int zcap = rd.cap[rd.z1band];
-                        int qq = zq + i;
-                        if (qq >= zcap) qq -= zcap;
                         z = *reinterpret_cast<const float4 *>(ring_smem + rd.soff[rd.z1band] +
-                                                              c * 16 + qq * kRingRowBytes);
+                                                              c * 16 + (zq + i) * kRingRowBytes);
                     } else {
                         z = *reinterpret_cast<const float4 *>(z1p + i * ldz1);
                     }
@@ -267,8 +282,8 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                 *reinterpret_cast<float4 *>(yp + i * ldy) = y;
             }
 #pragma unroll
-            for (int b = 0; b < kRingBandMax; ++b) {
-                if (b < rd.nb) {
+            for (int b = 0; b < (NB > 0 ? NB : kRingBandMax); ++b) {
+                if (NB > 0 || b < rd.nb) {
                     base[b] += kRingBR;
                     if (base[b] >= rd.cap[b]) base[b] -= rd.cap[b];
                 }
@@ -342,7 +357,7 @@ bool ring_plan(const DiaDesc &D, RingDesc *rd, size_t *smem) {
         rd->cap[b] = (rd->K[b] + 1) * kRingBR;
         rd->soff[b] = (int)off;
         rd->gfirst[b] = gfirst[b];
-        off += (size_t)rd->cap[b] * kRingRowBytes;
+        off += (size_t)(rd->cap[b] + kRingMirror) * kRingRowBytes;
         if (lo[b] <= 0 && hi[b] >= 0) {
             rd->z1band = b;
             rd->z1rel = (int)-lo[b];
@@ -364,44 +379,24 @@ bool ring_plan(const DiaDesc &D, RingDesc *rd, size_t *smem) {
     return off <= (size_t)kRingSmemMax;
 }
 
-}  // namespace
-
-int launch_dia_ring(cudaStream_t st, const DevMatrix *A, int w, const float *X, int64_t ldx,
-                    float *Y, int64_t ldy, const float *Z1, int64_t ldz1, const float *Z2,
-                    int64_t ldz2, double ca, double cb, double cc, int *status) {
-    if (!A || !A->dia32 || A->dia_ndiag <= 0 || !status) return CACG_ERR_UNSUPPORTED;
-    const int64_t n = A->n;
-    if (n <= 0 || n >= (1ll << 30) || w <= 0 || w % kRingCols != 0) return CACG_ERR_UNSUPPORTED;
-    if (!aligned16(X) || !aligned16(Y) || ldx % 4 || ldy % 4 || ldx < w || ldy < w)
-        return CACG_ERR_UNSUPPORTED;
-    if (Z1 && (!aligned16(Z1) || ldz1 % 4)) return CACG_ERR_UNSUPPORTED;
-    if (Z2 && (!aligned16(Z2) || ldz2 % 4)) return CACG_ERR_UNSUPPORTED;
-    if (A->dia_npad % 4 || !aligned16(A->dia32)) return CACG_ERR_UNSUPPORTED;
-    RingDesc rd;
-    size_t smem = 0;
-    if (!ring_plan(A->dia, &rd, &smem)) return CACG_ERR_UNSUPPORTED;
-    if (!(Z1 == X && ldz1 == ldx)) rd.z1band = -1;  // Z1 read from global memory
-    CUtensorMap tmx, tmv;
-    if (!encode_2d(&tmx, X, (uint64_t)w, (uint64_t)n, (uint64_t)ldx * 4, kRingCols, kRingBR,
-                   CU_TENSOR_MAP_L2_PROMOTION_NONE) ||
-        !encode_2d(&tmv, A->dia32, (uint64_t)A->dia_npad, (uint64_t)A->dia_ndiag,
-                   (uint64_t)A->dia_npad * 4, kRingBR, (uint32_t)A->dia_ndiag,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B))
-        return CACG_ERR_UNSUPPORTED;
-    static const int per_sm = [] {
-        cudaFuncSetAttribute(dia_ring_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kRingSmemMax);
-        return 0;
+template <int NB, int GPB, int G>
+int ring_launch(cudaStream_t st, const CUtensorMap &tmx, const CUtensorMap &tmm,
+                const CUtensorMap &tmv, int64_t n, const DiaDesc &desc, RingDesc &rd, size_t smem,
+                float *Y, int64_t ldy, const float *Z1, int64_t ldz1, const float *Z2, int64_t ldz2,
+                float ca, float cb, float cc, int *status) {
+    static const bool attr = [] {
+        cudaFuncSetAttribute(dia_ring_kernel<NB, GPB, G>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kRingSmemMax);
+        return true;
     }();
-    (void)per_sm;
+    (void)attr;
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dia_ring_kernel, kRingThreads, smem) !=
-            cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dia_ring_kernel<NB, GPB, G>,
+                                                      kRingThreads, smem) != cudaSuccess ||
         occ < 1) {
         cudaGetLastError();
         return CACG_ERR_UNSUPPORTED;
     }
-    rd.tiles = w / kRingCols;
     const int64_t grid0 = (int64_t)sm_count() * std::min(occ, 2);
     const int64_t nblk = (n + kRingBR - 1) / kRingBR;
     int kmax = 1;
@@ -411,10 +406,48 @@ int launch_dia_ring(cudaStream_t st, const DevMatrix *A, int w, const float *X, 
     rd.sb = (int)std::max<int64_t>(2 * kmax, (nblk + want - 1) / want);
     const int64_t nitems = (nblk + rd.sb - 1) / rd.sb * rd.tiles;
     const int64_t grid = std::min<int64_t>(grid0, nitems);
-    dia_ring_kernel<<<(unsigned)grid, kRingThreads, smem, st>>>(
-        tmx, tmv, n, nitems, A->dia, rd, Y, ldy, Z1, ldz1, Z2, ldz2, (float)ca, (float)cb,
-        (float)cc, status);
+    dia_ring_kernel<NB, GPB, G><<<(unsigned)grid, kRingThreads, smem, st>>>(
+        tmx, tmm, tmv, n, nitems, desc, rd, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc, status);
     return check_launch();
+}
+
+}  // namespace
+
+int launch_dia_ring(cudaStream_t st, const DevMatrix *A, int w, const float *X, int64_t ldx,
+                    float *Y, int64_t ldy, const float *Z1, int64_t ldz1, const float *Z2,
+                    int64_t ldz2, double ca, double cb, double cc, int *status) {
+    if (!A || !A->dia32 || A->dia_ndiag <= 0 || !status) return CACG_ERR_UNSUPPORTED;
+    const int64_t n = A->n;
+    // one 16-column tile: wider blocks (A Q) keep the unstaged kernel, which
+    // shares each row's values and window addressing over all columns
+    if (n <= 0 || n >= (1ll << 30) || w != kRingCols) return CACG_ERR_UNSUPPORTED;
+    if (!aligned16(X) || !aligned16(Y) || ldx % 4 || ldy % 4 || ldx < w || ldy < w)
+        return CACG_ERR_UNSUPPORTED;
+    if (Z1 && (!aligned16(Z1) || ldz1 % 4)) return CACG_ERR_UNSUPPORTED;
+    if (Z2 && (!aligned16(Z2) || ldz2 % 4)) return CACG_ERR_UNSUPPORTED;
+    if (A->dia_npad % 4 || !aligned16(A->dia32)) return CACG_ERR_UNSUPPORTED;
+    RingDesc rd;
+    size_t smem = 0;
+    if (!ring_plan(A->dia, &rd, &smem)) return CACG_ERR_UNSUPPORTED;
+    if (!(Z1 == X && ldz1 == ldx)) rd.z1band = -1;  // Z1 read from global memory
+    rd.tiles = w / kRingCols;
+    CUtensorMap tmx, tmm, tmv;
+    if (!encode_2d(&tmx, X, (uint64_t)w, (uint64_t)n, (uint64_t)ldx * 4, kRingCols, kRingBR,
+                   CU_TENSOR_MAP_L2_PROMOTION_NONE) ||
+        !encode_2d(&tmm, X, (uint64_t)w, (uint64_t)n, (uint64_t)ldx * 4, kRingCols, kRingMirror,
+                   CU_TENSOR_MAP_L2_PROMOTION_NONE) ||
+        !encode_2d(&tmv, A->dia32, (uint64_t)A->dia_npad, (uint64_t)A->dia_ndiag,
+                   (uint64_t)A->dia_npad * 4, kRingBR, (uint32_t)A->dia_ndiag,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B))
+        return CACG_ERR_UNSUPPORTED;
+    bool box333 = rd.nb == 3 && A->dia.ngroups == 9;
+    for (int b = 0; box333 && b < 3; ++b) box333 = rd.gfirst[b] == 3 * b;
+    for (int g = 0; box333 && g < 9; ++g) box333 = (rd.gdg[g] >> 8) == 3;
+    if (box333)
+        return ring_launch<3, 3, 3>(st, tmx, tmm, tmv, n, A->dia, rd, smem, Y, ldy, Z1, ldz1, Z2,
+                                    ldz2, (float)ca, (float)cb, (float)cc, status);
+    return ring_launch<0, 0, 0>(st, tmx, tmm, tmv, n, A->dia, rd, smem, Y, ldy, Z1, ldz1, Z2,
+                                ldz2, (float)ca, (float)cb, (float)cc, status);
 }
 
 }  // namespace cacg
