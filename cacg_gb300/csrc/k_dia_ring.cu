@@ -205,6 +205,20 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                            ring_smem + rd.voff + ((u + 1) & 1) * rd.vbytes, &bar[(u + 1) & 1]);
                 ++issued;
             }
+            // the recurrence operands from global memory do not wait for the
+            // staged rows: their loads go out before the barrier wait
+            const int64_t rbase = R0 + (int64_t)t * kRingBR + rowoff;
+            const int col = col0 + 4 * c;
+            const bool z1g = Z1 && rd.z1band < 0;
+            float4 z1v[kRingR], z2v[kRingR];
+#pragma unroll
+            for (int i = 0; i < kRingR; ++i) {
+                const bool in = rbase + i < n;
+                z1v[i] = z1g && in ? *reinterpret_cast<const float4 *>(Z1 + (rbase + i) * ldz1 + col)
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+                z2v[i] = Z2 && in ? *reinterpret_cast<const float4 *>(Z2 + (rbase + i) * ldz2 + col)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
             const bool ok = t5_mbar_wait(&bar[u & 1], (u >> 1) & 1);
             if (__syncthreads_or(!ok)) {
                 timeout = true;
@@ -250,11 +264,7 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                     }
                 }
             }
-            const int64_t rbase = R0 + (int64_t)t * kRingBR + rowoff;
-            const int col = col0 + 4 * c;
             float *yp = Y + rbase * ldy + col;
-            const float *z1p = Z1 ? Z1 + rbase * ldz1 + col : nullptr;
-            const float *z2p = Z2 ? Z2 + rbase * ldz2 + col : nullptr;
 #pragma unroll
             for (int i = 0; i < kRingR; ++i) {
                 if (rbase + i >= n) break;
@@ -265,7 +275,7 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                         z = *reinterpret_cast<const float4 *>(ring_smem + rd.soff[rd.z1band] +
                                                               c * 16 + (zq + i) * kRingRowBytes);
                     } else {
-                        z = *reinterpret_cast<const float4 *>(z1p + i * ldz1);
+                        z = z1v[i];
                     }
                     y.x = fmaf(cb, z.x, y.x);
                     y.y = fmaf(cb, z.y, y.y);
@@ -273,7 +283,7 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                     y.w = fmaf(cb, z.w, y.w);
                 }
                 if (Z2) {
-                    const float4 z = *reinterpret_cast<const float4 *>(z2p + i * ldz2);
+                    const float4 z = z2v[i];
                     y.x = fmaf(cc, z.x, y.x);
                     y.y = fmaf(cc, z.y, y.y);
                     y.z = fmaf(cc, z.z, y.z);
