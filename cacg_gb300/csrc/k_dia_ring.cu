@@ -429,7 +429,8 @@ int launch_dia_ring(cudaStream_t st, const DevMatrix *A, int w, const float *X, 
     if (!A || !A->dia32 || A->dia_ndiag <= 0 || !status) return CACG_ERR_UNSUPPORTED;
     const int64_t n = A->n;
     // one 16-column tile: wider blocks (A Q) keep the unstaged kernel, which
-    // shares each row's values and window addressing over all columns
+    // shares each row's values and window addressing over all columns (six
+    // staged tiles measured 0.93 ms against its 0.83 ms at 128^3, k = 96)
     if (n <= 0 || n >= (1ll << 30) || w != kRingCols) return CACG_ERR_UNSUPPORTED;
     if (!aligned16(X) || !aligned16(Y) || ldx % 4 || ldy % 4 || ldx < w || ldy < w)
         return CACG_ERR_UNSUPPORTED;
