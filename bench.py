@@ -351,7 +351,7 @@ def run_gpu_arm(args, w, rank, world):
                          "peak": hbm if bound == "hbm" else bf16,
                          "unit": "GB/s" if bound == "hbm" else "TFLOP/s",
                          "frac": (ach or 0) / (hbm if bound == "hbm" else bf16),
-                         "peak_source": src, "traffic": traffic_for(name),
+                         "peak_source": src, "traffic": traffic_for(name, n),
                          "per_launch_ms": per_launch_ms,
                          "algorithmic_bytes_per_launch": d["bytes"] / max(d["kernels"], 1)},
             "phases": phases,
@@ -399,13 +399,20 @@ def run_serving(args):
     return out
 
 
-def traffic_for(phase):
-    p = os.path.join(HERE, "profiles", "traffic.json")
-    try:
-        with open(p) as f:
-            return json.load(f).get(phase)
-    except Exception:
-        return None
+# DRAM bytes (read + write) per launch of each phase's kernel, from one ncu
+# capture of the 27-point 96^3 mixed solve (n = 884,736; per-kernel table
+# with the command in profiles/ncu_traffic_st27_96_m16.md); every figure is
+# linear in n at fixed m and s.
+TRAFFIC_96 = {"basis_spmm": 297.2e6, "aq_spmm": 737.2e6, "qupdate": 963.0e6,
+              "xrupdate": 1210.2e6, "gram": (679.8e6 + 736.7e6) / 2}
+TRAFFIC_96_N = 884736
+
+
+def traffic_for(phase, n):
+    """Per-launch DRAM bytes of `phase` for an n-row stencil of the family
+    the table was captured on (None for other phases)."""
+    t = TRAFFIC_96.get(phase)
+    return None if t is None else t * n / TRAFFIC_96_N
 
 
 def save_iterations(wname, it64, itmx):
