@@ -225,6 +225,13 @@ int launch_xrupdate_sl(cudaStream_t st, int64_t n, int k, int m, const float *Q,
                        float *S0, int64_t lds, float *R32, double *norms, double *ws,
                        Slices S0sl, Slices R32sl);
 // Same update with the k-term products accumulated in T (FP32 FMAs for float).
+// X/R update for m = 16, k a multiple of 16, FP32 Q and AQ (k_xr16.cu):
+// coalesced split-k rows, reduce-scatter over four lanes, FP64 only in the
+// additions into X and R.  CACG_ERR_UNSUPPORTED for other shapes.
+int launch_xrupdate_m16(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
+                        int64_t ldq, const double *alpha, double *X, double *R, float *S0,
+                        int64_t lds, float *R32, double *norms, double *ws);
+
 template <typename T>
 int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,
                          int64_t ldq, const double *alpha, double *X, double *R, T *S0,

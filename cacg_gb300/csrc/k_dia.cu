@@ -34,6 +34,7 @@
 
 #include "cacg_internal.cuh"
 #include "cacg_solver.h"
+#include "ff_util.cuh"
 
 namespace cacg {
 
@@ -205,41 +206,6 @@ int DevMatrix::build_dia(const cacg_csr *A, bool want_f32, cudaStream_t st) {
 }
 
 // -------------------------------------------------------------- float-float
-// x = hi + lo with FP32 hi, lo, using integer operations only (GB300's FP64
-// pipe runs at 1/64 of the FP32 rate): hi = x truncated to 24 significant
-// bits, lo = the next 29 bits rounded to FP32 (about 48 bits in all).
-// Values outside the normal FP32 exponent range give (float)x, 0.
-__device__ __forceinline__ void ff_split_bits(double x, float &hi, float &lo) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const int e = (int)((b >> 52) & 0x7FF);
-    const unsigned long long sgn = b >> 63;
-    if (e < 1023 - 126 + 24 || e > 1023 + 127) {  // tiny, huge, inf, NaN, zero
-        hi = (float)x;
-        lo = 0.f;
-        return;
-    }
-    const unsigned long long mant = b & ((1ull << 52) - 1);
-    hi = __uint_as_float((unsigned)((sgn << 31) | ((unsigned long long)(e - 1023 + 127) << 23) |
-                                    (mant >> 29)));
-    const unsigned rem = (unsigned)(mant & ((1u << 29) - 1));
-    // rem * 2^(e - 1075): the scale is a normal FP32 power of two in this range
-    const int se = e - 1075 + 127;
-    const float scale = se >= 1 ? __uint_as_float((unsigned)se << 23) : 0.f;
-    const float l = __uint2float_rn(rem) * scale;
-    lo = sgn ? -l : l;
-}
-
-// exact FP32 -> FP64 by bits for normal values (others through the cast)
-__device__ __forceinline__ double ff_widen(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xFF;
-    if (e == 0 || e == 0xFF) return (double)f;
-    const unsigned long long b = ((unsigned long long)(u >> 31) << 63) |
-                                 ((unsigned long long)(e - 127 + 1023) << 52) |
-                                 ((unsigned long long)(u & 0x7FFFFF) << 29);
-    return __longlong_as_double((long long)b);
-}
-
 __global__ void ff_split_kernel(int64_t count, const double *__restrict__ x,
                                 float *__restrict__ hi, float *__restrict__ lo) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;

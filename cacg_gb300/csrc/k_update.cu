@@ -396,6 +396,13 @@ int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, c
                          int64_t lds, float *R32, double *norms, double *ws) {
     if (m <= 0 || k <= 0) return CACG_ERR_ARG;
     if (norms && !ws) return CACG_ERR_ARG;
+    if constexpr (std::is_same<T, float>::value) {
+        if (m == 16) {
+            int rc = launch_xrupdate_m16(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms,
+                                         ws);
+            if (rc != CACG_ERR_UNSUPPORTED) return rc;
+        }
+    }
     if (direct_ok<T>(k, ldq, Q, AQ))
         return launch_xrupdate_direct<T>(st, n, k, m, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms,
                                          ws, Slices(), Slices());
