@@ -113,6 +113,16 @@ _SIGS = {
                                   C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "cacg_k_lu": (C.c_int, [C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                             C.c_void_p, C.c_void_p]),
+    # input files
+    "cacg_read_mtx": (C.c_int, [C.c_char_p, C.POINTER(CsrTypeLocal)]),
+    "cacg_csr_free": (None, [C.POINTER(CsrTypeLocal)]),
+    "cacg_csr_row_block": (C.c_int, [C.POINTER(CsrTypeLocal), C.c_int, C.c_int,
+                                     C.POINTER(CsrTypeLocal)]),
+    "cacg_read_csv": (C.c_int, [C.c_char_p, C.c_int64, C.c_int64, C.c_void_p,
+                                C.POINTER(C.c_int64)]),
+    "cacg_dense_row_block": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int, C.c_int,
+                                       C.POINTER(DenseType)]),
+    "cacg_dense_free": (None, [C.POINTER(DenseType)]),
     "cacg_launch_count": (C.c_int64, []),
     "cacg_profile_enable": (None, [C.c_int]),
     "cacg_profile_reset": (None, []),

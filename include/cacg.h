@@ -308,6 +308,47 @@ int cacg_server_stats(cacg_server *srv, int64_t *queued, int64_t *active,
                       int64_t *bytes_in_use);
 int cacg_server_destroy(cacg_server *srv);
 
+/* ----------------------------------------------------------- input files
+ * The reference's file inputs and its 1-D row-block split, on the host.
+ * Where the reference calls exit() or assert(), these return CACG_ERR_ARG
+ * (malformed input), CACG_ERR_UNSUPPORTED (valid file of a kind the
+ * reference refuses) or CACG_ERR_OOM, and leave the outputs zeroed. */
+
+/* Replaces readMtx_info_and_coo (src/readMTX.c:8-135) followed by
+ * Converter_Coo2Csr (src/matrixType.c:4-52): a Matrix Market coordinate file
+ * (field real, integer or pattern -- pattern entries read as 1.0; symmetry
+ * general, skew-symmetric read as stored, or symmetric with each
+ * off-diagonal entry followed by its mirror) into *out: 0-based long
+ * indices, a row's entries in file order, start = 0, arrays malloc'ed by the
+ * library (cacg_csr_free).  Array and complex files: CACG_ERR_UNSUPPORTED. */
+int cacg_read_mtx(const char *path, csrType_local *out);
+void cacg_csr_free(csrType_local *mat);
+
+/* Replaces the row split of Sparse_Csr_Matrix_Distribution
+ * (src/SparseMatrixDistribution.c:7-205): rank myid of numprocs gets rows
+ * [myid * (n / numprocs), ...), n / numprocs of them (the last rank also the
+ * remainder), row_start rebased to 0, global column indices, start = its
+ * first row.  A copy (cacg_csr_free). */
+int cacg_csr_row_block(const csrType_local *A, int myid, int numprocs,
+                       csrType_local *local);
+
+/* Replaces parseCSV (src/common.c:16-48): `rows` lines of `cols`
+ * comma-separated numbers (atof) into out (rows x cols, row-major).  Lines
+ * past `rows` are ignored; a shorter file leaves the remaining rows zero as
+ * the reference does (*rows_read, may be NULL, says how many were read); a
+ * line with another number of fields is CACG_ERR_ARG (the reference
+ * asserts).  No line-length limit (the reference reads 1024-byte lines). */
+int cacg_read_csv(const char *path, int64_t rows, int64_t cols, double *out,
+                  int64_t *rows_read);
+
+/* Replaces the split of GenVector_ReadCSV (src/GetRHS.c:124-208): rank
+ * myid's block of rows of a rows x cols row-major array, as a denseType with
+ * the reference's field values (start_idx = myid * cols * (rows / numprocs)).
+ * A copy (cacg_dense_free). */
+int cacg_dense_row_block(const double *global, int64_t rows, int64_t cols, int myid,
+                         int numprocs, denseType *local);
+void cacg_dense_free(denseType *d);
+
 /* ------------------------------------------------------------ generators */
 int64_t cacg_gen_rows(int kind, int64_t N);
 int64_t cacg_gen_nnz(int kind, int64_t N);

@@ -51,6 +51,12 @@ def ref_lib():
         lib.cacg_ref_gram.argtypes = [C.c_int, C.c_long, _f64, C.c_long, _f64, C.c_long, _f64]
         lib.cacg_ref_tallsmall.argtypes = [C.c_long, _f64, C.c_long, _f64, C.c_long, _f64]
         lib.cacg_ref_lu.argtypes = [C.c_long, _f64, C.c_long, _f64, _f64]
+        lib.cacg_ref_read_mtx.restype = C.c_long
+        lib.cacg_ref_read_mtx.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_long),
+                                          C.POINTER(C.c_long), C.POINTER(C.c_void_p),
+                                          C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
+        lib.cacg_ref_free.argtypes = [C.c_void_p]
+        lib.cacg_ref_parse_csv.argtypes = [C.c_char_p, C.c_long, C.c_long, _f64]
         _ref = lib
     return _ref
 
@@ -248,4 +254,33 @@ def ref_lu(M, RHS_):
 def ref_gerschgorin(rp, ci, v):
     out = np.empty(2)
     ref_lib().cacg_ref_gerschgorin(len(rp) - 1, _i64a(rp), _i64a(ci), v, out)
+    return out
+
+
+def ref_read_mtx(path):
+    """The reference's Matrix Market reader and COO -> CSR conversion
+    (src/readMTX.c:8-135, src/matrixType.c:4-52): (row_start, col_idx, values,
+    (num_rows, num_cols)).  Valid files only (the reference exits otherwise)."""
+    lib = ref_lib()
+    d, name = os.path.split(os.path.abspath(path))
+    nr, nc = C.c_long(), C.c_long()
+    prp, pci, pv = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    nnz = lib.cacg_ref_read_mtx(os.fsencode(d + os.sep), os.fsencode(name), C.byref(nr),
+                                C.byref(nc), C.byref(prp), C.byref(pci), C.byref(pv))
+    try:
+        rp = np.ctypeslib.as_array(C.cast(prp, C.POINTER(C.c_long)), (nr.value + 1,)).copy()
+        ci = (np.ctypeslib.as_array(C.cast(pci, C.POINTER(C.c_long)), (nnz,)).copy()
+              if nnz else np.zeros(0, np.int64))
+        v = (np.ctypeslib.as_array(C.cast(pv, C.POINTER(C.c_double)), (nnz,)).copy()
+             if nnz else np.zeros(0))
+    finally:
+        for p in (prp, pci, pv):
+            lib.cacg_ref_free(p)
+    return rp.astype(np.int64), ci.astype(np.int64), v, (nr.value, nc.value)
+
+
+def ref_parse_csv(path, rows, cols):
+    """The reference's parseCSV (src/common.c:16-48)."""
+    out = np.zeros((rows, cols))
+    ref_lib().cacg_ref_parse_csv(os.fsencode(path), rows, cols, out)
     return out

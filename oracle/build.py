@@ -2,7 +2,8 @@
 
 1. ``oracle/_ref/libcacgref.so`` -- the reference sclc/cacg solver sources
    (src/bcbcgKernel.c, src/cbcgKernel.c, src/common.c, src/BLAS3.c,
-   src/DLSsolvers.c, src/MatrixOperations.c, src/matrixType.c) compiled with
+   src/DLSsolvers.c, src/MatrixOperations.c, src/matrixType.c, src/readMTX.c
+   and the Matrix Market library it vendors, src/mmio.c) compiled with
    gcc against the project-written MPI shim (oracle/mpi_shim) and the harness
    (oracle/ref_harness.c).  The sources are staged into ``oracle/_ref/src``
    (git-ignored) because two constants must become variables:
@@ -42,6 +43,8 @@ REF_C_FILES = [
     "DLSsolvers.c",
     "MatrixOperations.c",
     "matrixType.c",
+    "readMTX.c",
+    "mmio.c",
 ]
 CFLAGS = ["-O2", "-fPIC", "-std=gnu99", "-ffp-contract=off", "-w"]
 

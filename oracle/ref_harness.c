@@ -276,3 +276,41 @@ void cacg_ref_lu(long k, const double *M, long r, const double *RHS, double *Y) 
     denseType Yd = make_dense(k, r, Y);
     LUsolver_v1_KeeplhsMat(&Yd, Md, Rd, 0, 1);
 }
+
+/* ---------------------------------------------------------- input files */
+void readMtx_info_and_coo(char *path, char *name, matInfo *info, cooType *mat);
+void Converter_Coo2Csr(cooType src, csrType_local *target, matInfo *mat_info);
+void parseCSV(char *filename, double **output, long numRows, long numCols);
+
+/* src/readMTX.c:8-135 then src/matrixType.c:4-52, as
+ * Sparse_Csr_Matrix_Distribution runs them on rank 0
+ * (src/SparseMatrixDistribution.c:43-51).  The arrays are the reference's
+ * own allocations (release with cacg_ref_free).  The reference exits on a
+ * malformed file: call it with valid files only. */
+long cacg_ref_read_mtx(const char *dir, const char *name, long *nrows, long *ncols,
+                       long **rp, long **ci, double **v) {
+    matInfo info;
+    cooType coo;
+    csrType_local csr;
+    readMtx_info_and_coo((char *)dir, (char *)name, &info, &coo);
+    Converter_Coo2Csr(coo, &csr, &info);
+    free(coo.rowIdx);
+    free(coo.colIdx);
+    free(coo.coodata);
+    *nrows = csr.num_rows;
+    *ncols = csr.num_cols;
+    *rp = csr.row_start;
+    *ci = csr.col_idx;
+    *v = csr.csrdata;
+    return csr.nnz;
+}
+
+void cacg_ref_free(void *p) { free(p); }
+
+/* src/common.c:16-48: rows x cols values into out */
+void cacg_ref_parse_csv(const char *path, long rows, long cols, double *out) {
+    double *buf = NULL;
+    parseCSV((char *)path, &buf, rows, cols);
+    memcpy(out, buf, (size_t)rows * cols * sizeof(double));
+    free(buf);
+}

@@ -122,6 +122,30 @@ def test_overwrite_x0_solves_in_place(lib):
     assert np.array_equal(Xc, Xi)
 
 
+def test_mtx_csv_inputs_through_dropin(lib):
+    """The reference driver's input path (src/main.c: Matrix Market matrix,
+    CSV right-hand sides): the library's readers feed the bcbcg_v1 drop-in;
+    the oracle solves the same inputs.  The matrix rows are in file order
+    (unsorted), so the CSR kernels run."""
+    import os
+    io = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "io")
+    rp, ci, v, (n, nc) = cg.read_mtx(os.path.join(io, "lap2d_12_sym.mtx"))
+    B, got = cg.read_csv(os.path.join(io, "rhs_144x4.csv"), n, 4)
+    assert got == n and nc == n
+    eps = 1e-8 * float(np.linalg.norm(B[:, 0]))
+    X = np.zeros_like(B)
+    cg.set_dropin_maxit(400)
+    try:
+        cg.bcbcg_v1(rp, ci, v, B, X, 4, eps)
+        st, it = cg.last_status(), cg.last_iterations()
+    finally:
+        cg.set_dropin_maxit(0)
+    assert st == 0
+    Xo, ito, _ = _ref(rp, ci, v, B, 4, eps, None, 400)
+    assert abs(it - ito) <= 1
+    assert _rel(X, Xo) <= 1e-6
+
+
 def test_mixed_lanczos_bounds_varcoef(lib):
     rp, ci, v = cg.gen_matrix("varcoef2d", 48, shift=1e-6, sigma=1.5, seed=3)
     n = len(rp) - 1
