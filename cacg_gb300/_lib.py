@@ -20,6 +20,7 @@ TOL_ABS_COL0, TOL_REL_ALL = 0, 1
 FP64, MIXED = 0, 1
 GRAM_AUTO, GRAM_FMA, GRAM_DMMA, GRAM_TC, GRAM_TC_SLICES, GRAM_TC5 = 0, 1, 2, 3, 4, 5
 SPMM_AUTO, SPMM_CSR, SPMM_DIA_UNSTAGED = 0, 1, 2
+ALG_CACG, ALG_BCG = 0, 1
 RESID_AUTO, RESID_FP64 = 0, 1
 VAL_F64, VAL_F32 = 0, 1
 
@@ -37,7 +38,8 @@ class CacgParams(C.Structure):
                 ("gram_variant", C.c_int32), ("lanczos_seed", C.c_uint64),
                 ("stream", C.c_void_p), ("use_graph", C.c_int32),
                 ("exact_updates", C.c_int32), ("spmm_format", C.c_int32),
-                ("residual_precision", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("residual_precision", C.c_int32), ("algorithm", C.c_int32),
+                ("reserved", C.c_int32 * 3)]
 
 
 class CacgResult(C.Structure):
@@ -74,6 +76,7 @@ _SIGS = {
                        C.c_int]),
     "bcbcg_v1": (None, [CsrTypeLocal, DenseType, DenseType, C.c_long, C.c_double, C.c_int,
                         C.c_int]),
+    "bcg_v1": (None, [CsrTypeLocal, DenseType, DenseType, C.c_double, C.c_int, C.c_int]),
     "cacg_last_status": (C.c_int, []),
     "cacg_last_iterations": (C.c_int, []),
     "cacg_set_dropin_maxit": (None, [C.c_int]),

@@ -237,7 +237,8 @@ int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, c
                          int64_t ldq, const double *alpha, double *X, double *R, T *S0,
                          int64_t lds, float *R32, double *norms, double *ws);
 
-// Small LU (Crout, U unit diagonal, no pivoting); F holds k*k + k doubles.
+// Small LU (Crout, U unit diagonal, no pivoting); F holds 2 k*k + k doubles
+// (the factor, its reciprocal pivots, and the factor transposed for the solves).
 int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *status);
 int launch_lu_solve(cudaStream_t st, int k, const double *F, int r, const double *RHS,
                     double *Y);

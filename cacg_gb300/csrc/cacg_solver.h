@@ -68,6 +68,15 @@ int launch_dia_ring(cudaStream_t st, const DevMatrix *A, int w, const float *X, 
                     float *Y, int64_t ldy, const float *Z1, int64_t ldz1, const float *Z2,
                     int64_t ldz2, double ca, double cb, double cc, int *status);
 
+// Per-thread pinned host scratch of at least `bytes` (reused across calls).
+double *pinned_scratch(size_t bytes);
+
+// Block CG (bcg_v1, src/bcgKernel.c:22-462), FP64, on the same kernels
+// (bcg.cu).  tol_mode, tol, maxit, gram_variant, spmm_format and stream of p
+// apply; s, bounds and the mixed-precision fields do not.
+int solve_bcg_on_device(const DevMatrix *A, const double *B, double *X, int m,
+                        const cacg_params *p, cacg_result *res);
+
 // Device bytes of one solve's state (S, Q, AQ, R, small matrices, reduction
 // workspaces), the admission cost of a request.
 size_t solve_workspace_bytes(int64_t n, int m, int s, int prec, bool lanczos);

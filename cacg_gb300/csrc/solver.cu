@@ -264,7 +264,7 @@ struct PinnedScratch {
         if (p) cudaFreeHost(p);
     }
 };
-static double *pinned_scratch(size_t bytes) {
+double *pinned_scratch(size_t bytes) {
     static thread_local PinnedScratch ps;
     if (ps.bytes < bytes) {
         if (ps.p) cudaFreeHost(ps.p);
@@ -986,6 +986,8 @@ int solve_on_device(const DevMatrix *A, const double *B, double *X, int m,
                     const cacg_params *pin, cacg_result *res, void *ws_external,
                     size_t ws_external_bytes) {
     if (!A || !B || !X || m <= 0 || m > 256 || !pin || !res) return CACG_ERR_ARG;
+    if (pin->algorithm == CACG_ALG_BCG) return solve_bcg_on_device(A, B, X, m, pin, res);
+    if (pin->algorithm != CACG_ALG_CACG) return CACG_ERR_ARG;
     keep_pool_memory();
     cacg_params p = *pin;
     if (p.s < 2 || p.maxit < 0 || (p.precision != CACG_FP64 && p.precision != CACG_MIXED))
@@ -1208,7 +1210,8 @@ int cacg_last_iterations(void) { return t_last_iters; }
 void cacg_set_dropin_maxit(int maxit) { g_dropin_maxit.store(maxit > 0 ? maxit : 0); }
 
 static void dropin(csrType_local mat, denseType B, denseType X, long s, double epsilon,
-                   int numprocs, int default_maxit, const char *name) {
+                   int numprocs, int default_maxit, const char *name,
+                   int algorithm = CACG_ALG_CACG) {
     t_last_iters = 0;
     if (numprocs != 1) {
         fprintf(stderr, "%s (libcacg): one rank per GPU only; numprocs=%d unsupported\n", name,
@@ -1250,6 +1253,7 @@ static void dropin(csrType_local mat, denseType B, denseType X, long s, double e
     int ov = g_dropin_maxit.load();
     p.maxit = ov > 0 ? ov : default_maxit;
     p.precision = CACG_FP64;
+    p.algorithm = algorithm;
     cacg_result r;
     memset(&r, 0, sizeof r);
     int rc = cacg_solve(&A, B.data, X.data, (int32_t)m, &p, &r);
@@ -1267,6 +1271,13 @@ void bcbcg_v1(csrType_local mat, denseType B, denseType X, long s, double epsilo
               int numprocs) {
     (void)myid;
     dropin(mat, B, X, s, epsilon, numprocs, 100, "bcbcg_v1");  // src/bcbcgKernel.c:3
+}
+
+void bcg_v1(csrType_local mat, denseType B, denseType X, double epsilon, int myid,
+            int numprocs) {
+    (void)myid;
+    // s is not a bcg_v1 argument; 2 passes the drop-in's argument check only
+    dropin(mat, B, X, 2, epsilon, numprocs, 1000, "bcg_v1", CACG_ALG_BCG);  // src/bcgKernel.c:2
 }
 
 }  // extern "C"

@@ -67,6 +67,7 @@ class Params:
                                     # | "dia_unstaged" (DIA without shared-memory staging)
     residual: str = "auto"          # mixed: "auto" (float-float replacements on DIA) | "fp64"
     use_graph: bool = False         # replay captured outer iterations (non-default stream)
+    algorithm: str = "cacg"         # "cacg" (cbcg_v1 / bcbcg_v1) | "bcg" (block CG, FP64)
 
     def to_c(self) -> L.CacgParams:
         p = L.CacgParams()
@@ -96,6 +97,7 @@ class Params:
                          "dia_unstaged": L.SPMM_DIA_UNSTAGED}[self.spmm_format]
         p.residual_precision = {"auto": L.RESID_AUTO, "fp64": L.RESID_FP64}[self.residual]
         p.use_graph = 1 if self.use_graph else 0
+        p.algorithm = {"cacg": L.ALG_CACG, "bcg": L.ALG_BCG}[self.algorithm]
         return p
 
 
@@ -166,7 +168,10 @@ def _dropin(fn, row_start, col_idx, csrdata, B, X, s, epsilon, myid, numprocs):
         B = B[:, None]
     Xv = X if X.ndim == 2 else X.reshape(-1, 1)
     mat, Bd, Xd, keep = _ref_structs(row_start, col_idx, csrdata, B, Xv)
-    fn(mat, Bd, Xd, s, epsilon, myid, numprocs)
+    if s is None:  # bcg_v1 takes no s
+        fn(mat, Bd, Xd, epsilon, myid, numprocs)
+    else:
+        fn(mat, Bd, Xd, s, epsilon, myid, numprocs)
 
 
 def cbcg_v1(row_start, col_idx, csrdata, B, X, s, epsilon, myid=0, numprocs=1):
@@ -177,6 +182,11 @@ def cbcg_v1(row_start, col_idx, csrdata, B, X, s, epsilon, myid=0, numprocs=1):
 def bcbcg_v1(row_start, col_idx, csrdata, B, X, s, epsilon, myid=0, numprocs=1):
     """Drop-in for bcbcg_v1 (src/bcbcgKernel.h:22); X is updated in place."""
     _dropin(L.lib().bcbcg_v1, row_start, col_idx, csrdata, B, X, s, epsilon, myid, numprocs)
+
+
+def bcg_v1(row_start, col_idx, csrdata, B, X, epsilon, myid=0, numprocs=1):
+    """Drop-in for bcg_v1, block CG (src/bcgKernel.h:22); X is updated in place."""
+    _dropin(L.lib().bcg_v1, row_start, col_idx, csrdata, B, X, None, epsilon, myid, numprocs)
 
 
 def last_status() -> int:

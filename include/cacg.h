@@ -66,6 +66,9 @@ extern "C" {
                             (tcgen05.mma, accumulator in tensor memory, float-float
                             sums across 256-row groups) */
 
+#define CACG_ALG_CACG 0 /* s-step Chebyshev-basis CG: cbcg_v1 (m = 1) / bcbcg_v1 */
+#define CACG_ALG_BCG 1  /* block CG, bcg_v1 (src/bcgKernel.c:22) */
+
 #define CACG_SPMM_AUTO 0
 #define CACG_SPMM_CSR 1 /* always the CSR kernels */
 #define CACG_SPMM_DIA_UNSTAGED 2 /* the DIA view, read through the caches only (no
@@ -131,7 +134,9 @@ typedef struct cacg_params {
                                    periodic residual replacements in float-float
                                    (about 44 bits, FP32 pipe) unless FP64 is asked
                                    for; convergence checks are always FP64 */
-    int32_t reserved[4];
+    int32_t algorithm;    /* CACG_ALG_*: the s-step Chebyshev solvers (default) or
+                             block CG (bcg_v1; FP64 only, s and bounds unused) */
+    int32_t reserved[3];
 } cacg_params;
 
 typedef struct cacg_result {
@@ -162,6 +167,14 @@ void cbcg_v1(csrType_local mat, denseType B, denseType X, long s, double epsilon
  * (src/bcbcgKernel.c:3). */
 void bcbcg_v1(csrType_local mat, denseType B, denseType X, long s, double epsilon,
               int myid, int numprocs);
+/* Replaces void bcg_v1(csrType_local mat, denseType B, denseType X,
+ * double epsilon, int myid, int numprocs), src/bcgKernel.h:22: block CG (no
+ * s-step basis), FP64, X in/out, stops when ||R(:,0)|| < epsilon -- tested
+ * on the residual before the iteration's R update, after X has moved, as
+ * src/bcgKernel.c:311-424 does -- or after 1000 iterations
+ * (src/bcgKernel.c:2). */
+void bcg_v1(csrType_local mat, denseType B, denseType X, double epsilon, int myid,
+            int numprocs);
 /* Status of the calling thread's last drop-in call (they return void). */
 int cacg_last_status(void);
 /* Iterations / final ||R(:,0)|| of the calling thread's last drop-in call. */

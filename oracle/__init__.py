@@ -192,9 +192,11 @@ def _i64a(a):
     return np.ascontiguousarray(a, np.int64)
 
 
-def ref_solve(rp, ci, v, B, X0, s, eps, bounds=None, maxit=100, nranks=1, quiet=True):
-    """Run the reference cbcg_v1 (m == 1) / bcbcg_v1 (m > 1).  Returns
-    (X, iterations, history, seconds)."""
+def ref_solve(rp, ci, v, B, X0, s, eps, bounds=None, maxit=100, nranks=1, quiet=True,
+              algorithm="cacg"):
+    """Run the reference cbcg_v1 (m == 1) / bcbcg_v1 (m > 1), or with
+    algorithm="bcg" the block CG bcg_v1 (src/bcgKernel.c:22; s unused).
+    Returns (X, iterations, history, seconds)."""
     lib = ref_lib()
     if lib is None:
         raise RuntimeError("reference oracle unavailable")
@@ -204,7 +206,7 @@ def ref_solve(rp, ci, v, B, X0, s, eps, bounds=None, maxit=100, nranks=1, quiet=
     hist = np.zeros(max(maxit, 1))
     secs = C.c_double(0.0)
     mode, lo, hi = (0, 0.0, 0.0) if bounds is None else (1, bounds[0], bounds[1])
-    solver = 1 if m == 1 else 2
+    solver = 3 if algorithm == "bcg" else (1 if m == 1 else 2)
     it = lib.cacg_ref_solve(solver, nranks, n, _i64a(rp), _i64a(ci), v, B, X, m, s, eps,
                             mode, lo, hi, maxit, hist, len(hist), 1 if quiet else 0,
                             C.byref(secs))
@@ -284,3 +286,43 @@ def ref_parse_csv(path, rows, cols):
     out = np.zeros((rows, cols))
     ref_lib().cacg_ref_parse_csv(os.fsencode(path), rows, cols, out)
     return out
+
+
+def port_bcg(rp, ci, v, B, X0, eps, maxit=1000):
+    """Numpy restatement of bcg_v1 (src/bcgKernel.c:22-462), FP64: returns
+    (X, iterations, history of ||R(:,0)||).  Order of operations as in the
+    reference: X += P alpha, then the test on the residual before this
+    iteration's update (:311-424), then R -= AP alpha, beta and P (:427-457).
+    The m x m solves use numpy's LAPACK solver, not the reference's no-pivot
+    Crout LU (src/DLSsolvers.c:6-91): results agree to rounding."""
+    rp = np.asarray(rp, np.int64)
+    ci = np.asarray(ci, np.int64)
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp))
+
+    def spmm(Xm):
+        Y = np.zeros_like(Xm)
+        np.add.at(Y, rows, v[:, None] * Xm[ci])
+        return Y
+
+    B = np.asarray(B, np.float64)
+    X = np.array(X0, np.float64, copy=True)
+    R = B - spmm(X)
+    P = R.copy()
+    G = R.T @ R
+    hist = []
+    it = 0
+    for it in range(1, maxit + 1):
+        AP = spmm(P)
+        alpha = np.linalg.solve(P.T @ AP, G)
+        X += P @ alpha
+        rn = float(np.sqrt(R[:, 0] @ R[:, 0]))
+        hist.append(rn)
+        if rn < eps:
+            break
+        R -= AP @ alpha
+        G2 = R.T @ R
+        beta = np.linalg.solve(G, G2)
+        P = R + P @ beta
+        G = G2
+    return X, it, np.array(hist)

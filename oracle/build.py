@@ -1,14 +1,15 @@
 """Build recipe for the two CPU oracles (test infrastructure, never the product).
 
 1. ``oracle/_ref/libcacgref.so`` -- the reference sclc/cacg solver sources
-   (src/bcbcgKernel.c, src/cbcgKernel.c, src/common.c, src/BLAS3.c,
-   src/DLSsolvers.c, src/MatrixOperations.c, src/matrixType.c, src/readMTX.c
-   and the Matrix Market library it vendors, src/mmio.c) compiled with
+   (src/bcbcgKernel.c, src/cbcgKernel.c, src/bcgKernel.c, src/common.c,
+   src/BLAS3.c, src/DLSsolvers.c, src/MatrixOperations.c, src/matrixType.c,
+   src/readMTX.c and the Matrix Market library it vendors, src/mmio.c) compiled with
    gcc against the project-written MPI shim (oracle/mpi_shim) and the harness
    (oracle/ref_harness.c).  The sources are staged into ``oracle/_ref/src``
-   (git-ignored) because two constants must become variables:
-   ``#define MAXITER 100`` (src/bcbcgKernel.c:3) and
-   ``#define CBCG_MAXITER 1000`` (src/cbcgKernel.c:2) are rewritten to read
+   (git-ignored) because three constants must become variables:
+   ``#define MAXITER 100`` (src/bcbcgKernel.c:3),
+   ``#define CBCG_MAXITER 1000`` (src/cbcgKernel.c:2) and
+   ``#define BCG_MAXITER 1000`` (src/bcgKernel.c:2) are rewritten to read
    ``cacg_ref_maxiter``.  No other line changes.  Missing prototypes in the
    reference (e.g. get_same_shape_denseType used by src/bcbcgKernel.c:57
    without matrixType.h) are supplied with ``-include``.  Staging happens
@@ -45,6 +46,7 @@ REF_C_FILES = [
     "matrixType.c",
     "readMTX.c",
     "mmio.c",
+    "bcgKernel.c",
 ]
 CFLAGS = ["-O2", "-fPIC", "-std=gnu99", "-ffp-contract=off", "-w"]
 
@@ -74,6 +76,10 @@ def stage_reference(ref_src: str = REF_SRC_DEFAULT) -> bool:
             text, k = re.subn(r"^#define CBCG_MAXITER 1000\b",
                               "#define CBCG_MAXITER cacg_ref_maxiter", text, flags=re.M)
             assert k == 1, "CBCG_MAXITER line not found"
+        if name == "bcgKernel.c":
+            text, k = re.subn(r"^#define BCG_MAXITER 1000\b",
+                              "#define BCG_MAXITER cacg_ref_maxiter", text, flags=re.M)
+            assert k == 1, "BCG_MAXITER line not found"
         dst = os.path.join(REF_STAGE, name)
         if os.path.exists(dst):
             with open(dst) as f:
@@ -103,7 +109,7 @@ def build_reference(ref_src: str = REF_SRC_DEFAULT, force: bool = False) -> str 
         extra = []
         if name == "common.c":
             extra = ["-Dgerschgorin_v1=gerschgorin_v1_ref"]
-        if name in ("bcbcgKernel.c", "cbcgKernel.c"):
+        if name in ("bcbcgKernel.c", "cbcgKernel.c", "bcgKernel.c"):
             extra = ["-Dnorm2square_dist_denseMat_col_n=cacg_ref_norm_hook"]
         src = os.path.join(REF_STAGE, name)
         obj = os.path.join(objdir, name[:-2] + ".o")

@@ -85,8 +85,27 @@ void cacg_ref_norm_hook(denseType mat, double *result, long n, int myid, int num
     }
 }
 
+void bcg_v1(csrType_local mat, denseType B, denseType X, double epsilon, int myid,
+            int numprocs);
+
+/* src/bcgKernel.c:597 bcg_Scalapack_qr (never called by bcg_v1) refers to
+ * BLACS/ScaLAPACK, which this build does not have: these stand-ins satisfy
+ * the link and stop the process if that path were ever reached. */
+static void no_scalapack(void) {
+    fprintf(stderr, "oracle: ScaLAPACK path of src/bcgKernel.c is not built\n");
+    abort();
+}
+void Cblacs_pinfo(long *a, long *b) { (void)a; (void)b; no_scalapack(); }
+void Cblacs_get(long a, long b, long *c) { (void)a; (void)b; (void)c; no_scalapack(); }
+void Cblacs_gridinfo(long a, long *b, long *c, long *d, long *e) {
+    (void)a; (void)b; (void)c; (void)d; (void)e; no_scalapack();
+}
+void Cblacs_gridmap(void) { no_scalapack(); }
+void descinit_(void) { no_scalapack(); }
+long numroc_(void) { no_scalapack(); return 0; }
+
 typedef struct {
-    int solver; /* 1 = cbcg_v1, 2 = bcbcg_v1 */
+    int solver; /* 1 = cbcg_v1, 2 = bcbcg_v1, 3 = bcg_v1 */
     long n, m, s;
     const long *row_ptr, *col_idx;
     const double *val, *B;
@@ -130,6 +149,8 @@ static void rank_body(int rank, void *p) {
     double t0 = MPI_Wtime();
     if (j->solver == 1)
         cbcg_v1(A, B, X, j->s, j->eps, rank, np);
+    else if (j->solver == 3)
+        bcg_v1(A, B, X, j->eps, rank, np);
     else
         bcbcg_v1(A, B, X, j->s, j->eps, rank, np);
     MPI_Barrier(MPI_COMM_WORLD);
@@ -143,7 +164,8 @@ static void rank_body(int rank, void *p) {
 }
 
 /*
- * Run the reference solver.  solver: 1 = cbcg_v1 (m must be 1), 2 = bcbcg_v1.
+ * Run the reference solver.  solver: 1 = cbcg_v1 (m must be 1), 2 = bcbcg_v1,
+ * 3 = bcg_v1 (block CG, no s).
  * bounds_mode 0 = the reference's Gerschgorin bounds, 1 = [lmin, lmax].
  * eps is the reference's absolute threshold on ||R(:,0)||.  X is in/out.
  * hist (capacity hist_cap, may be NULL) receives ||R(:,0)|| per outer
