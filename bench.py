@@ -309,6 +309,19 @@ def run_gpu_arm(args, w, rank, world):
     fp64_value = m / (f0.elapsed_time(f1) * 1e-3)
     assert info64["status"] == 0 and info64["true_relres_max"] <= w["tol"]
 
+    # block CG (bcg_v1, FP64, no s-step basis) on the same inputs: the
+    # non-communication-avoiding baseline on the same kernels
+    pbcg = cg.Params(algorithm="bcg", tol=w["tol"], maxit=5000, precision="fp64")
+    barrier()
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record()
+    infobcg = solve(pbcg)
+    g1.record()
+    barrier()
+    bcg_value = m / (g0.elapsed_time(g1) * 1e-3)
+    assert infobcg["status"] == 0 and infobcg["true_relres_max"] <= w["tol"]
+
     # end to end through the C ABI with host buffers (cacg_solve): A, B and
     # the initial X go host->device, X comes back, every step
     # the caller's X (in/out, as cbcg_v1's X) is reset to x0 = 0 every step
@@ -345,6 +358,7 @@ def run_gpu_arm(args, w, rank, world):
                        "iterations_mixed": iters_mixed, "iterations_fp64": info64["iterations"],
                        "true_relres_max": relres},
             "fp64_value": fp64_value, "mixed_vs_fp64": value / world / fp64_value,
+            "bcg_fp64_value": bcg_value, "bcg_iterations": infobcg["iterations"],
             "spmm_hbm_gbs": spmm.get("gbs"),
             "spmm_hbm_frac": (spmm.get("gbs") or 0) / hbm,
             "roofline": {"kernel": name, "bound": bound, "achieved": ach,
