@@ -290,8 +290,8 @@ def run_gpu_arm(args, w, rank, world):
         if l_.value == 0:
             continue
         name = lib.cacg_profile_name(ph).decode()
-        phases[name] = {"ms": ms_.value, "launch_groups": None, "kernels": l_.value,
-                        "bytes": b_.value, "flops": f_.value}
+        phases[name] = {"ms": ms_.value, "calls": lib.cacg_profile_calls(ph),
+                        "kernels": l_.value, "bytes": b_.value, "flops": f_.value}
     for name, d in phases.items():
         secs = d["ms"] * 1e-3
         d["gbs"] = d["bytes"] / secs / 1e9 if secs > 0 else None
@@ -344,7 +344,7 @@ def run_gpu_arm(args, w, rank, world):
         hbm, bf16, src = peaks()
         dom = max(phases.items(), key=lambda kv: kv[1]["ms"])
         name, d = dom
-        per_launch_ms = d["ms"] / max(d["kernels"], 1)
+        per_call_ms = d["ms"] / max(d["calls"], 1)
         bound = "tensor" if name == "gram" and d.get("tensor") else "hbm"
         ach = d["gbs"]
         spmm = phases.get("basis_spmm", {})
@@ -366,8 +366,8 @@ def run_gpu_arm(args, w, rank, world):
                          "unit": "GB/s" if bound == "hbm" else "TFLOP/s",
                          "frac": (ach or 0) / (hbm if bound == "hbm" else bf16),
                          "peak_source": src, "traffic": traffic_for(name, n),
-                         "per_launch_ms": per_launch_ms,
-                         "algorithmic_bytes_per_launch": d["bytes"] / max(d["kernels"], 1)},
+                         "per_call_ms": per_call_ms,
+                         "algorithmic_bytes_per_call": d["bytes"] / max(d["calls"], 1)},
             "phases": phases,
             "e2e": {"value": m / e2e_s, "unit": "RHS/s", "h2d_bytes_per_step": hb,
                     "d2h_bytes_per_step": db},
@@ -413,18 +413,20 @@ def run_serving(args):
     return out
 
 
-# DRAM bytes (read + write) per launch of each phase's kernel, from one ncu
-# capture of the 27-point 96^3 mixed solve (n = 884,736; per-kernel table
-# with the command in profiles/ncu_traffic_st27_96_m16.md); every figure is
-# linear in n at fixed m and s.
+# DRAM bytes (read + write) per call of each phase (one Gram product = the
+# tcgen05 split-K kernel and its reduction; one X/R update = the update and
+# its norm sum), from one ncu capture of the 27-point 96^3 mixed solve
+# (n = 884,736; per-kernel table with the command in
+# profiles/ncu_traffic_st27_96_m16.md); every figure is linear in n at fixed
+# m and s.
 TRAFFIC_96 = {"basis_spmm": 297.2e6, "aq_spmm": 737.2e6, "qupdate": 963.0e6,
-              "xrupdate": 1210.2e6, "gram": (679.8e6 + 736.7e6) / 2}
+              "xrupdate": 1210.2e6 + 0.1e6, "gram": (679.8e6 + 736.7e6) / 2 + 12.2e6}
 TRAFFIC_96_N = 884736
 
 
 def traffic_for(phase, n):
-    """Per-launch DRAM bytes of `phase` for an n-row stencil of the family
-    the table was captured on (None for other phases)."""
+    """Per-call DRAM bytes of `phase` for an n-row stencil of the family the
+    table was captured on (None for other phases)."""
     t = TRAFFIC_96.get(phase)
     return None if t is None else t * n / TRAFFIC_96_N
 

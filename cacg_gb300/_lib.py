@@ -131,6 +131,7 @@ _SIGS = {
     "cacg_profile_reset": (None, []),
     "cacg_profile_get": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                    C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "cacg_profile_calls": (C.c_int64, [C.c_int]),
     "cacg_profile_name": (C.c_char_p, [C.c_int]),
     # server
     "cacg_server_create": (C.c_int, [C.POINTER(CacgServerConfig), C.POINTER(C.c_void_p)]),

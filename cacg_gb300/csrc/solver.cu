@@ -301,6 +301,7 @@ static std::mutex g_prof_mu;
 struct PhaseAcc {
     double ms = 0, bytes = 0, flops = 0;
     int64_t launches = 0;
+    int64_t calls = 0;  // timed begin/end pairs (one product, one update, ...)
 };
 static PhaseAcc g_prof[CACG_NUM_PHASES];
 
@@ -356,6 +357,7 @@ struct Profiler {
                 a.bytes += p.bytes;
                 a.flops += p.flops;
                 a.launches += p.launches;
+                a.calls += 1;
             }
             cudaGetLastError();
             pool.push_back(p.a);
@@ -1104,6 +1106,12 @@ int cacg_profile_get(int phase, double *ms, int64_t *launches, double *bytes, do
     if (bytes) *bytes = a.bytes;
     if (flops) *flops = a.flops;
     return CACG_OK;
+}
+
+int64_t cacg_profile_calls(int phase) {
+    if (phase < 0 || phase >= CACG_NUM_PHASES) return 0;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    return g_prof[phase].calls;
 }
 
 const char *cacg_profile_name(int phase) {

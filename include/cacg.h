@@ -297,6 +297,9 @@ int64_t cacg_launch_count(void);
 void cacg_profile_enable(int on);
 void cacg_profile_reset(void);
 int cacg_profile_get(int phase, double *ms, int64_t *launches, double *bytes, double *flops);
+/* Timed calls of a phase (one Gram product, one basis step, ...; a call may
+ * launch more than one kernel, e.g. a split-K product and its reduction). */
+int64_t cacg_profile_calls(int phase);
 const char *cacg_profile_name(int phase);
 
 /* ----------------------------------------------------------- serving loop */
