@@ -28,15 +28,13 @@
 // the three bands read (N^2 rows apart) is an L2 hit after its first read.
 // The waits on the TMA barriers are bounded: on expiry the CTA sets
 // kStatusTimeout, waits (bounded) for the loads it has in flight and returns.
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
 #include <algorithm>
 #include <vector>
 
 #include "cacg_internal.cuh"
 #include "cacg_solver.h"
 #include "tc5_util.cuh"
+#include "tma_util.cuh"
 
 namespace cacg {
 
@@ -71,26 +69,6 @@ struct RingDesc {
     int gdg[kDiaMax];              // group g: first diagonal | diagonals << 8
 };
 
-__device__ __forceinline__ void ring_expect_tx(uint64_t *bar, unsigned bytes) {
-    asm volatile(
-        "{\n"
-        ".reg .b64 st;\n"
-        "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n"
-        "}\n" ::"r"(t5_smem_u32(bar)),
-        "r"(bytes)
-        : "memory");
-}
-
-// 2-D tiled TMA load of the box at (x, y) (elements; x innermost) into dst
-__device__ __forceinline__ void ring_tma2d(void *dst, const CUtensorMap *map, int x, int y,
-                                           uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
-        "[%0], [%1, {%2, %3}], [%4];\n" ::"r"(t5_smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(t5_smem_u32(bar))
-        : "memory");
-}
-
 // Loads of block t of an item (first: the K_b start-up chunks of every band)
 // and its values, completing on *bar.  A chunk that goes to slot 0 also
 // fills the ring's mirror rows (its first kRingMirror rows, after the last
@@ -106,18 +84,18 @@ __device__ __forceinline__ void ring_issue(unsigned char *sm, const RingDesc &rd
             bytes += kRingBR * kRingRowBytes +
                      (j % (rd.K[b] + 1) == 0 ? kRingMirror * kRingRowBytes : 0);
     }
-    ring_expect_tx(bar, bytes);
+    tma_expect_tx(bar, bytes);
     for (int b = 0; b < rd.nb; ++b) {
         const int j0 = first ? 0 : t + rd.K[b] - 1, j1 = first ? rd.K[b] : j0 + 1;
         for (int j = j0; j < j1; ++j) {
             const int slot = j % (rd.K[b] + 1);
             const int y = (int)(R0 + rd.lo[b] + (int64_t)j * kRingBR);
-            ring_tma2d(sm + rd.soff[b] + slot * (kRingBR * kRingRowBytes), tmx, col0, y, bar);
+            tma_load_2d(sm + rd.soff[b] + slot * (kRingBR * kRingRowBytes), tmx, col0, y, bar);
             if (slot == 0)
-                ring_tma2d(sm + rd.soff[b] + rd.cap[b] * kRingRowBytes, tmm, col0, y, bar);
+                tma_load_2d(sm + rd.soff[b] + rd.cap[b] * kRingRowBytes, tmm, col0, y, bar);
         }
     }
-    ring_tma2d(vdst, tmv, (int)(R0 + (int64_t)t * kRingBR), 0, bar);
+    tma_load_2d(vdst, tmv, (int)(R0 + (int64_t)t * kRingBR), 0, bar);
 }
 
 // One group of G adjacent diagonals: the window of R + G - 1 staged rows
@@ -308,37 +286,6 @@ __global__ void __launch_bounds__(kRingThreads, 2)
     }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                             &q) != cudaSuccess ||
-            q != cudaDriverEntryPointSuccess) {
-            cudaGetLastError();
-            p = nullptr;
-        }
-        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }();
-    return fn;
-}
-
-// FP32 2-D map: `inner` elements per row (contiguous), `outer` rows
-// `row_bytes` apart; box box_in x box_out; zero fill outside.
-bool encode_2d(CUtensorMap *m, const void *base, uint64_t inner, uint64_t outer,
-               uint64_t row_bytes, uint32_t box_in, uint32_t box_out,
-               CUtensorMapL2promotion promo) {
-    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
-    if (!fn) return false;
-    cuuint64_t dims[2] = {inner, outer};
-    cuuint64_t strides[1] = {row_bytes};
-    cuuint32_t box[2] = {box_in, box_out};
-    cuuint32_t es[2] = {1, 1};
-    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims, strides, box,
-              es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, promo,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 // Bands, rings and shared-memory layout for the matrix's diagonals; false
 // when they do not fit.
 bool ring_plan(const DiaDesc &D, RingDesc *rd, size_t *smem) {
@@ -443,13 +390,14 @@ int launch_dia_ring(cudaStream_t st, const DevMatrix *A, int w, const float *X, 
     if (!(Z1 == X && ldz1 == ldx)) rd.z1band = -1;  // Z1 read from global memory
     rd.tiles = w / kRingCols;
     CUtensorMap tmx, tmm, tmv;
-    if (!encode_2d(&tmx, X, (uint64_t)w, (uint64_t)n, (uint64_t)ldx * 4, kRingCols, kRingBR,
-                   CU_TENSOR_MAP_L2_PROMOTION_NONE) ||
-        !encode_2d(&tmm, X, (uint64_t)w, (uint64_t)n, (uint64_t)ldx * 4, kRingCols, kRingMirror,
-                   CU_TENSOR_MAP_L2_PROMOTION_NONE) ||
-        !encode_2d(&tmv, A->dia32, (uint64_t)A->dia_npad, (uint64_t)A->dia_ndiag,
-                   (uint64_t)A->dia_npad * 4, kRingBR, (uint32_t)A->dia_ndiag,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B))
+    const CUtensorMapSwizzle nosw = CU_TENSOR_MAP_SWIZZLE_NONE;
+    if (!tma_encode_2d(&tmx, X, (uint64_t)w, (uint64_t)n, (uint64_t)ldx * 4, kRingCols, kRingBR,
+                       nosw, CU_TENSOR_MAP_L2_PROMOTION_NONE) ||
+        !tma_encode_2d(&tmm, X, (uint64_t)w, (uint64_t)n, (uint64_t)ldx * 4, kRingCols,
+                       kRingMirror, nosw, CU_TENSOR_MAP_L2_PROMOTION_NONE) ||
+        !tma_encode_2d(&tmv, A->dia32, (uint64_t)A->dia_npad, (uint64_t)A->dia_ndiag,
+                       (uint64_t)A->dia_npad * 4, kRingBR, (uint32_t)A->dia_ndiag, nosw,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B))
         return CACG_ERR_UNSUPPORTED;
     bool box333 = rd.nb == 3 && A->dia.ngroups == 9;
     for (int b = 0; box333 && b < 3; ++b) box333 = rd.gfirst[b] == 3 * b;

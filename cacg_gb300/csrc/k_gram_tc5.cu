@@ -39,6 +39,7 @@
 
 #include "cacg_internal.cuh"
 #include "tc5_util.cuh"
+#include "tma_util.cuh"
 
 namespace cacg {
 
@@ -314,6 +315,269 @@ __global__ void __launch_bounds__(kT5Threads, 1)
     for (int q = 0; q < HC; ++q) out[q] = (double)acc_hi[q] + (double)acc_lo[q];
 }
 
+// ---------------------------------------------------------------------------
+// MN-major variant (the default where the operands allow TMA): raw FP32 rows
+// arrive as 32 x 32 boxes (128 bytes a row, 128-byte swizzle) by 2-D TMA
+// loads that one thread issues; the slices are stored MN-major (a core-matrix
+// row = 8 consecutive columns of one input row), so a thread converts a unit
+// (8 columns of one row) with two 16-byte shared loads, the split and three
+// 16-byte stores, without the column gather a K-major tile needs.  The 128-B
+// swizzle puts the 16-byte chunk c of row k at chunk c ^ (k & 7), so the 8
+// rows a quarter warp reads fall on distinct banks; the MN-major core matrix
+// rows (16 bytes at (k & 7) * 16) are conflict-free for the same 8 rows.
+// Descriptors (no swizzle, MN-major): SBO = 128 B between 8-column groups,
+// LBO = (MN / 8) * 128 B between 8-row (K) groups; instruction descriptor
+// with the A and B transpose bits.
+constexpr int kT5mBox = 32;                          // rows and FP32 columns of a box
+constexpr unsigned kT5mBoxBytes = kT5mBox * kT5mBox * 4;  // 4 KB
+
+template <int NC8>
+__global__ void __launch_bounds__(kT5Threads, 1)
+    gram_tc5m_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant__ CUtensorMap tmR1,
+                     const __grid_constant__ CUtensorMap tmR2, int64_t n, int64_t rows_per_chunk,
+                     int ka, int kb1, int kb2, int BA, int tilesB, int tmem_half, int stages,
+                     double *__restrict__ part, int *__restrict__ status) {
+    constexpr int BB = 16 * NC8;
+    constexpr int HC = BB / 2;  // accumulator columns per thread
+    constexpr unsigned a_bytes = kT5M * kT5KT * 2, b_bytes = BB * kT5KT * 2;
+    constexpr unsigned buf_bytes = 3 * (a_bytes + b_bytes);
+    constexpr unsigned lbo_a = (kT5M / 8) * 128, lbo_b = (BB / 8) * 128;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // [slices buf 0][slices buf 1][ring: stages x boxes x 4 KB, 1 KB aligned][mbar][tmem slot]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tile_a = blockIdx.y / tilesB, tile_b = blockIdx.y % tilesB;
+    const int a0 = tile_a * BA, b0 = tile_b * BB;
+    const int nbl = (BA + kT5mBox - 1) / kT5mBox;
+    const int r1end = min(b0 + BB, kb1);
+    const int nbr1 = b0 < kb1 ? (r1end - b0 + kT5mBox - 1) / kT5mBox : 0;
+    const int r2beg = max(b0, kb1), r2end = min(b0 + BB, kb1 + kb2);
+    const int nbr2 = r2end > r2beg ? (r2end - r2beg + kT5mBox - 1) / kT5mBox : 0;
+    const int c2 = r2beg - kb1;  // first R2 column of this tile's boxes
+    const int nbox = nbl + nbr1 + nbr2;
+    const unsigned ring_off = (2 * buf_bytes + 1023) / 1024 * 1024;
+    unsigned char *ring = smem_raw + ring_off;
+    const unsigned stage_bytes = (unsigned)nbox * kT5mBoxBytes;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(ring + (size_t)stages * stage_bytes);
+    uint64_t *full = mbar + 2;  // one per ring stage
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(full + stages);
+
+    const int64_t rbeg = (int64_t)blockIdx.x * rows_per_chunk;
+    const int64_t rend = min(n, rbeg + rows_per_chunk);
+    const int64_t nsteps = rend > rbeg ? (rend - rbeg + kT5KT - 1) / kT5KT : 0;
+
+    for (unsigned i = tid; i < 2 * buf_bytes / 16; i += kT5Threads)
+        reinterpret_cast<uint4 *>(smem_raw)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        t5_mbar_init(&mbar[0], 1);
+        t5_mbar_init(&mbar[1], 1);
+        for (int q = 0; q < stages; ++q) t5_mbar_init(&full[q], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         t5_smem_u32(tmem_slot)),
+                     "r"(2 * tmem_half));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const unsigned tmem = *tmem_slot;
+
+    // ---- TMA loads of one step (thread 0): the tile's L, R1, R2 boxes
+    int64_t issued = 0;  // steps whose loads were issued (thread 0)
+    auto issue_loads = [&](int64_t j) {
+        if (j >= nsteps) return;
+        const int q = (int)(j % stages);
+        unsigned char *dst = ring + (size_t)q * stage_bytes;
+        const int row0 = (int)(rbeg + j * kT5KT);
+        tma_expect_tx(&full[q], stage_bytes);
+        for (int b = 0; b < nbl; ++b)
+            tma_load_2d(dst + b * kT5mBoxBytes, &tmL, a0 + kT5mBox * b, row0, &full[q]);
+        for (int b = 0; b < nbr1; ++b)
+            tma_load_2d(dst + (nbl + b) * kT5mBoxBytes, &tmR1, b0 + kT5mBox * b, row0, &full[q]);
+        for (int b = 0; b < nbr2; ++b)
+            tma_load_2d(dst + (nbl + nbr1 + b) * kT5mBoxBytes, &tmR2, c2 + kT5mBox * b, row0,
+                        &full[q]);
+        issued = j + 1;
+    };
+
+    // ---- conversion units: (row k of the step, 8-column octet o)
+    int usrc[kT5MaxUnits], uch[kT5MaxUnits], udst[kT5MaxUnits], uslice[kT5MaxUnits], urow[kT5MaxUnits];
+    const int noct = (BA + BB) / 8;
+#pragma unroll
+    for (int u = 0; u < kT5MaxUnits; ++u) {
+        const int id = tid + u * kT5Threads;
+        usrc[u] = -1;
+        uch[u] = 0;
+        udst[u] = 0;
+        uslice[u] = 0;
+        urow[u] = 0;
+        if (id < kT5KT * noct) {
+            const int k = id % kT5KT, o = id / kT5KT;
+            int box, col;  // box of the stage, column of the octet in the box
+            if (o < BA / 8) {
+                box = (8 * o) / kT5mBox;
+                col = (8 * o) % kT5mBox;
+                udst[u] = o * 128 + (k / 8) * (int)lbo_a + (k % 8) * 16;
+                uslice[u] = (int)a_bytes;
+            } else {
+                const int cb = 8 * (o - BA / 8);  // column of the tile's B block
+                if (b0 + cb < kb1) {
+                    box = nbl + cb / kT5mBox;
+                    col = cb % kT5mBox;
+                } else {
+                    const int rel = b0 + cb - kb1 - c2;
+                    box = nbl + nbr1 + rel / kT5mBox;
+                    col = rel % kT5mBox;
+                }
+                udst[u] = 3 * (int)a_bytes + (o - BA / 8) * 128 + (k / 8) * (int)lbo_b + (k % 8) * 16;
+                uslice[u] = (int)b_bytes;
+            }
+            // an octet past the operand's columns (tile wider than the matrix)
+            // has no box: it converts zeros
+            usrc[u] = box < nbox ? box * (int)kT5mBoxBytes + k * 128 : -2;
+            uch[u] = col / 4;  // first of the octet's two 16-byte chunks
+            urow[u] = k;
+        }
+    }
+    auto convert = [&](int64_t j, int buf) {
+        const unsigned char *src = ring + (size_t)(j % stages) * stage_bytes;
+        unsigned char *dbase = smem_raw + buf * buf_bytes;
+        const int64_t r0 = rbeg + j * kT5KT;
+#pragma unroll
+        for (int u = 0; u < kT5MaxUnits; ++u) {
+            if (usrc[u] == -1) continue;
+            const int sw = urow[u] & 7;
+            float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+            // rows of the next chunk (or past n) and octets without a box stay zero
+            if (usrc[u] >= 0 && r0 + urow[u] < rend) {
+                v0 = *reinterpret_cast<const float4 *>(src + usrc[u] + ((uch[u] ^ sw) << 4));
+                v1 = *reinterpret_cast<const float4 *>(src + usrc[u] + (((uch[u] + 1) ^ sw) << 4));
+            }
+            unsigned hw[4], mw[4], lw[4];
+            t5_split2(v0.x, v0.y, hw[0], mw[0], lw[0]);
+            t5_split2(v0.z, v0.w, hw[1], mw[1], lw[1]);
+            t5_split2(v1.x, v1.y, hw[2], mw[2], lw[2]);
+            t5_split2(v1.z, v1.w, hw[3], mw[3], lw[3]);
+            unsigned char *d = dbase + udst[u];
+            *reinterpret_cast<uint4 *>(d) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+            *reinterpret_cast<uint4 *>(d + uslice[u]) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+            *reinterpret_cast<uint4 *>(d + 2 * uslice[u]) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+    };
+
+    // ---- float-float accumulator row of this thread (as gram_tc5_kernel)
+    const int quad = warp & 3, half = warp >> 2;
+    const int row_t = 32 * quad + lane;
+    float acc_hi[HC], acc_lo[HC];
+#pragma unroll
+    for (int q = 0; q < HC; ++q) acc_hi[q] = acc_lo[q] = 0.f;
+    auto flush = [&](int64_t step) {
+        const unsigned tb = (unsigned)(((step / kT5Flush) & 1) * tmem_half);
+#pragma unroll
+        for (int c8 = 0; c8 < NC8; ++c8) {
+            float v[8];
+            t5_ld8(tmem + ((unsigned)(32 * quad) << 16) + tb + (unsigned)(half * HC + 8 * c8), v);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                float &hi = acc_hi[8 * c8 + q];
+                const float s = hi + v[q];
+                const float bp = s - hi;
+                acc_lo[8 * c8 + q] += (hi - (s - bp)) + (v[q] - bp);
+                hi = s;
+            }
+        }
+    };
+    auto group_end = [&](int64_t e) { return e % kT5Flush == kT5Flush - 1 || e == nsteps - 1; };
+
+    const unsigned idesc = t5_idesc(kT5M, BB) | (1u << 15) | (1u << 16);  // A, B MN-major
+    auto issue_mma = [&](int64_t j) {  // thread 0: the 12 MMAs of step j
+        const int buf = (int)(j & 1);
+        const unsigned abase = t5_smem_u32(smem_raw + buf * buf_bytes);
+        const unsigned bbase = abase + 3 * a_bytes;
+        const unsigned d = tmem + (unsigned)(((j / kT5Flush) & 1) * tmem_half);
+        unsigned accumulate = (j % kT5Flush) != 0;
+        const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+        for (int pr = 0; pr < 6; ++pr) {
+#pragma unroll
+            for (int kk = 0; kk < kT5KT / 16; ++kk) {
+                const uint64_t ad = t5_desc_lbo(abase + pa[pr] * a_bytes + 2 * kk * lbo_a, lbo_a, 128);
+                const uint64_t bd = t5_desc_lbo(bbase + pb[pr] * b_bytes + 2 * kk * lbo_b, lbo_b, 128);
+                t5_mma(d, ad, bd, idesc, accumulate);
+                accumulate = 1;
+            }
+        }
+        t5_commit(&mbar[buf]);
+    };
+
+    int timed_out = 0, aborted = 0;
+    int64_t last_committed = -1;  // thread 0
+    if (tid == 0)
+        for (int j = 0; j < stages - 1; ++j) issue_loads(j);
+    for (int64_t i = 0; i <= nsteps; ++i) {
+        if (i < nsteps && !timed_out &&
+            !t5_mbar_wait(&full[i % stages], (unsigned)((i / stages) & 1))) {
+            if (lane == 0) atomicOr(status, kStatusTimeout);
+            timed_out = 1;
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        aborted = __syncthreads_or(timed_out);
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (aborted) break;
+        if (i >= 1 && tid == 0) {
+            issue_mma(i - 1);
+            last_committed = i - 1;
+        }
+        if (i == nsteps) break;
+        if (tid == 0) issue_loads(i + stages - 1);  // the stage of step i-1, read before the barrier
+        if (i >= 2) {
+            if (!__all_sync(0xffffffffu, t5_mbar_wait(&mbar[i & 1], (unsigned)(((i - 2) >> 1) & 1)))) {
+                if (lane == 0) atomicOr(status, kStatusTimeout);
+                timed_out = 1;
+            } else {
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                if (group_end(i - 2)) flush(i - 2);
+            }
+        }
+        convert(i, (int)(i & 1));
+    }
+    bool ok = !aborted;
+    if (!aborted && nsteps > 0) {
+        const int64_t last = nsteps - 1;
+        ok = __all_sync(0xffffffffu, t5_mbar_wait(&mbar[last & 1], (unsigned)((last >> 1) & 1)));
+        if (!ok && lane == 0) atomicOr(status, kStatusTimeout);
+    } else if (aborted && tid == 0) {
+        // bounded waits for the MMAs and the loads still in flight
+        if (last_committed >= 0)
+            t5_mbar_wait(&mbar[last_committed & 1], (unsigned)((last_committed >> 1) & 1));
+        for (int64_t j = 0; j < issued; ++j)
+            if (j >= issued - stages) t5_mbar_wait(&full[j % stages], (unsigned)((j / stages) & 1));
+    }
+    if (nsteps > 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (!aborted) {
+            if (ok && nsteps >= 2 && group_end(nsteps - 2)) flush(nsteps - 2);
+            if (ok) flush(nsteps - 1);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    const int bad = __syncthreads_or(!ok);
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                     "r"(2 * tmem_half));
+    }
+    if (bad || row_t >= BA) return;
+    double *out = part + ((size_t)blockIdx.x * gridDim.y + blockIdx.y) * (size_t)BA * BB +
+                  (size_t)row_t * BB + half * HC;
+#pragma unroll
+    for (int q = 0; q < HC; ++q) out[q] = (double)acc_hi[q] + (double)acc_lo[q];
+}
+
 struct T5Plan {
     int BA, BB, tilesA, tilesB, nchunks, tmem_half;
     int64_t rows_per_chunk;
@@ -369,6 +633,75 @@ int launch_gram_reduce(cudaStream_t st, const double *part, int nchunks, int nti
                        int BB, int tilesB, int ka, int kb, int kb1, double *C1, int ldc1,
                        double *C2, int ldc2);
 
+template <int NC8>
+static void t5m_set_attr() {
+    static const bool once = [] {
+        cudaFuncSetAttribute(gram_tc5m_kernel<NC8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)max_smem_optin());
+        return true;
+    }();
+    (void)once;
+}
+
+// The MN-major / TMA kernel; CACG_ERR_UNSUPPORTED when the operands do not
+// allow TMA boxes (16-byte aligned bases and row strides; an R1/R2 boundary
+// on an 8-column octet) or the ring does not fit.
+static int launch_tc5m(cudaStream_t st, const T5Plan &p, int64_t n, const float *L, int64_t ldl,
+                       int ka, const float *R1, int64_t ldr1, int kb1, const float *R2,
+                       int64_t ldr2, int kb2, double *ws, int *status) {
+    if (n <= 0 || n >= (1ll << 31) - 4096) return CACG_ERR_UNSUPPORTED;
+    if (ldl % 4 || ldr1 % 4 || (kb2 > 0 && (ldr2 % 4 || kb1 % 8)) || !aligned16(L) ||
+        !aligned16(R1) || (kb2 > 0 && !aligned16(R2)))
+        return CACG_ERR_UNSUPPORTED;
+    const CUtensorMapSwizzle sw = CU_TENSOR_MAP_SWIZZLE_128B;
+    const CUtensorMapL2promotion pr = CU_TENSOR_MAP_L2_PROMOTION_L2_256B;
+    CUtensorMap tmL, tmR1, tmR2;
+    if (!tma_encode_2d(&tmL, L, (uint64_t)ka, (uint64_t)n, (uint64_t)ldl * 4, kT5mBox, kT5mBox,
+                       sw, pr) ||
+        !tma_encode_2d(&tmR1, R1, (uint64_t)kb1, (uint64_t)n, (uint64_t)ldr1 * 4, kT5mBox,
+                       kT5mBox, sw, pr))
+        return CACG_ERR_UNSUPPORTED;
+    if (kb2 > 0) {
+        if (!tma_encode_2d(&tmR2, R2, (uint64_t)kb2, (uint64_t)n, (uint64_t)ldr2 * 4, kT5mBox,
+                           kT5mBox, sw, pr))
+            return CACG_ERR_UNSUPPORTED;
+    } else {
+        tmR2 = tmR1;  // never loaded
+    }
+    const size_t buf = 3 * ((size_t)kT5M * kT5KT * 2 + (size_t)p.BB * kT5KT * 2);
+    const size_t ring_off = (2 * buf + 1023) / 1024 * 1024;
+    const int nbox_max = (p.BA + kT5mBox - 1) / kT5mBox + (p.BB + kT5mBox - 1) / kT5mBox + 1;
+    int stages = 4;
+    size_t smem = 0;
+    for (; stages >= 2; --stages) {
+        smem = ring_off + (size_t)stages * nbox_max * kT5mBoxBytes + (2 + stages) * 8 + 16;
+        if (smem <= max_smem_optin()) break;
+    }
+    if (stages < 2) return CACG_ERR_UNSUPPORTED;
+    dim3 grid(p.nchunks, p.tilesA * p.tilesB);
+#define T5M_CASE(NC)                                                                               \
+    case NC:                                                                                       \
+        t5m_set_attr<NC>();                                                                        \
+        gram_tc5m_kernel<NC><<<grid, kT5Threads, smem, st>>>(tmL, tmR1, tmR2, n, p.rows_per_chunk, \
+                                                             ka, kb1, kb2, p.BA, p.tilesB,         \
+                                                             p.tmem_half, stages, ws, status);     \
+        break;
+    switch (p.BB / 16) {
+        T5M_CASE(1)
+        T5M_CASE(2)
+        T5M_CASE(3)
+        T5M_CASE(4)
+        T5M_CASE(5)
+        T5M_CASE(6)
+        T5M_CASE(7)
+        T5M_CASE(8)
+        default:
+            return CACG_ERR_UNSUPPORTED;
+    }
+#undef T5M_CASE
+    return check_launch();
+}
+
 int launch_gram_tc5(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int ka,
                     const float *R1, int64_t ldr1, int kb1, const float *R2, int64_t ldr2,
                     int kb2, double *C1, int ldc1, double *C2, int ldc2, double *ws,
@@ -379,7 +712,10 @@ int launch_gram_tc5(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int
     T5Plan p = plan_tc5(n, ka, kb);
     const size_t need = (size_t)p.nchunks * p.tilesA * p.tilesB * p.BA * p.BB * sizeof(double);
     if (!ws || need > ws_bytes) return CACG_ERR_ARG;
-    if (n > 0) {
+    int mrc = launch_tc5m(st, p, n, L, ldl, ka, R1, ldr1, kb1, R2, ldr2, kb2, ws, status);
+    if (mrc != CACG_ERR_UNSUPPORTED) {
+        if (mrc != CACG_OK) return mrc;
+    } else if (n > 0) {
         if (p.smem > max_smem_optin()) return CACG_ERR_UNSUPPORTED;
         const int vec16 = (ldl % 4 == 0) && (ldr1 % 4 == 0) && (kb2 == 0 || ldr2 % 4 == 0) &&
                           (kb1 % 4 == 0) && aligned16(L) && aligned16(R1) &&

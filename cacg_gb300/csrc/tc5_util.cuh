@@ -38,6 +38,13 @@ __device__ __forceinline__ uint64_t t5_desc(unsigned saddr, unsigned sbo) {
            ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
 }
 
+// Same with an explicit LBO (MN-major operands: LBO = bytes between 8-row K
+// groups, SBO = bytes between 8-column MN groups).
+__device__ __forceinline__ uint64_t t5_desc_lbo(unsigned saddr, unsigned lbo, unsigned sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
 // Instruction descriptor of kind::f16: D FP32, A and B bf16, both K-major,
 // M x N tile.
 __host__ __device__ constexpr unsigned t5_idesc(int M, int N) {
@@ -118,6 +125,16 @@ __device__ __forceinline__ void t5_ld8(unsigned taddr, float (&v)[8]) {
     for (int q = 0; q < 8; ++q) v[q] = __uint_as_float(r[q]);
 }
 
+__device__ __forceinline__ void t5_ld4(unsigned taddr, float (&v)[4]) {
+    unsigned r[4];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = __uint_as_float(r[q]);
+}
+
 __device__ __forceinline__ void t5_fence_before() {
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
 }
@@ -145,28 +162,20 @@ __device__ __forceinline__ int t5_bar_or(int id, int count, int pred) {
     return out;
 }
 
-// x0, x1 -> three bf16x2 words (high, middle, low slices), x = h + m + l
-// exactly.  Veltkamp splitting with sigma = 2^16 + 1 rounds to the nearest
-// 8-significant-bit value (the same slices as a round-to-nearest bf16
-// conversion at each split) using FP32 multiplies and subtractions only;
-// every slice is then exactly a bf16, i.e. the upper half of its FP32 bits,
-// and two of them pack into a word with one byte permute.  The _rn
-// intrinsics keep the compiler from contracting s*y - y into an FMA, which
-// would break the split.
-__device__ __forceinline__ float t5_veltkamp_hi(float y) {
-    const float g = __fmul_rn(65537.0f, y);
-    return __fsub_rn(g, __fsub_rn(g, y));
-}
+// x0, x1 -> three bf16x2 words (high, middle, low slices; round-to-nearest
+// at each split, so x = h + m + l up to the last slice's rounding).
 __device__ __forceinline__ void t5_split2(float x0, float x1, unsigned &hw, unsigned &mw,
                                           unsigned &lw) {
-    const float h0 = t5_veltkamp_hi(x0), h1 = t5_veltkamp_hi(x1);
-    const float r0 = __fsub_rn(x0, h0), r1 = __fsub_rn(x1, h1);
-    const float m0 = t5_veltkamp_hi(r0), m1 = t5_veltkamp_hi(r1);
-    const float l0 = __fsub_rn(r0, m0), l1 = __fsub_rn(r1, m1);
-    // low half: element 0, high half: element 1 (the __nv_bfloat162 layout)
-    hw = __byte_perm(__float_as_uint(h0), __float_as_uint(h1), 0x7632);
-    mw = __byte_perm(__float_as_uint(m0), __float_as_uint(m1), 0x7632);
-    lw = __byte_perm(__float_as_uint(l0), __float_as_uint(l1), 0x7632);
+    const float2 v = make_float2(x0, x1);
+    const __nv_bfloat162 h = __float22bfloat162_rn(v);
+    const float2 hf = __bfloat1622float2(h);
+    const float2 r1 = make_float2(v.x - hf.x, v.y - hf.y);
+    const __nv_bfloat162 m = __float22bfloat162_rn(r1);
+    const float2 mf = __bfloat1622float2(m);
+    const __nv_bfloat162 l = __float22bfloat162_rn(make_float2(r1.x - mf.x, r1.y - mf.y));
+    hw = t5_bits(h);
+    mw = t5_bits(m);
+    lw = t5_bits(l);
 }
 
 }  // namespace cacg

@@ -383,3 +383,23 @@ def test_gram_tc5_padded_rows_partial_chunks(lib, torch_cuda, n):
                          ptr(C), 7, None)
     assert rc == 0
     assert relerr(host(C), want) <= 4e-6
+
+
+@pytest.mark.parametrize("n", [31, 8191, 100003])
+def test_gram_tc5_tma_subblocks(lib, torch_cuda, n):
+    """tcgen05 Gram through TMA boxes on sub-blocks of wider arrays (row
+    strides 48, 32 and 12; the tensor maps end at the block's last column, so
+    the boxes zero-fill the rest): L = 40 of 48 columns, R1 = 24 of 32,
+    R2 = 8 of 12."""
+    torch = torch_cuda
+    Lw = O.gen_rhs("normal", n, 48, 21).astype(np.float32)
+    R1w = O.gen_rhs("normal", n, 32, 22).astype(np.float32)
+    R2w = O.gen_rhs("normal", n, 12, 23).astype(np.float32)
+    want = O.port_gram(Lw[:, :40].astype(np.float64),
+                       np.hstack([R1w[:, :24], R2w[:, :8]]).astype(np.float64))
+    d = {k_: dev(torch, a) for k_, a in dict(L=Lw, R1=R1w, R2=R2w).items()}
+    C = torch.zeros((40, 32), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_gram(F32, 5, n, ptr(d["L"]), 48, 40, ptr(d["R1"]), 32, 24, ptr(d["R2"]), 12,
+                         8, ptr(C), 32, None)
+    assert rc == 0
+    assert relerr(host(C), want) <= 4e-6
