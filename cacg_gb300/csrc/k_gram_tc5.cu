@@ -331,19 +331,39 @@ __global__ void __launch_bounds__(kT5Threads, 1)
 constexpr int kT5mBox = 32;                          // rows and FP32 columns of a box
 constexpr unsigned kT5mBoxBytes = kT5mBox * kT5mBox * 4;  // 4 KB
 
+constexpr int kT5wConvWarps = 16;                  // converter warps
+constexpr int kT5wConv = 32 * kT5wConvWarps;          // converter threads
+constexpr int kT5wThreads = kT5wConv + 64;            // + a loader warp and an MMA warp
+constexpr int kT5wUnits = 2;                          // conversion units per converter thread
+constexpr int kT5wNB = 2;                             // bf16 slice buffers
+
+// Warp-specialised pipeline, no CTA-wide barrier per step:
+//   loader (thread 512): waits empty[q], issues step j's TMA boxes into ring
+//     stage q = j % stages, completing on full[q];
+//   converters (warps 0-15): wait full[q] and sfree[b] (b = j % 2), split the
+//     stage into slice buffer b, fence the stores to the async proxy, arrive
+//     on sfull[b] and empty[q]; two steps after a group's last step they read
+//     its FP32 sum from TMEM (gdone[g & 1]) into the float-float registers and
+//     arrive on gfree[g & 1];
+//   MMA issuer (thread 544): waits sfull[b] (and gfree before a group reuses
+//     a TMEM buffer), issues the 12 MMAs, commits to sfree[b] and, at a
+//     group's end, to gdone[g & 1].
+// Every wait is bounded and also ends when another role has set the abort
+// flag; a role that times out sets kStatusTimeout and the flag, the loader
+// and the issuer then wait (bounded) for their own loads and MMAs in flight.
 template <int NC8>
-__global__ void __launch_bounds__(kT5Threads, 1)
+__global__ void __launch_bounds__(kT5wThreads, 1)
     gram_tc5m_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant__ CUtensorMap tmR1,
                      const __grid_constant__ CUtensorMap tmR2, int64_t n, int64_t rows_per_chunk,
                      int ka, int kb1, int kb2, int BA, int tilesB, int tmem_half, int stages,
                      double *__restrict__ part, int *__restrict__ status) {
     constexpr int BB = 16 * NC8;
-    constexpr int HC = BB / 2;  // accumulator columns per thread
+    constexpr int HC = BB / 4;  // accumulator columns per converter thread (a quarter row)
     constexpr unsigned a_bytes = kT5M * kT5KT * 2, b_bytes = BB * kT5KT * 2;
     constexpr unsigned buf_bytes = 3 * (a_bytes + b_bytes);
     constexpr unsigned lbo_a = (kT5M / 8) * 128, lbo_b = (BB / 8) * 128;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // [slices buf 0][slices buf 1][ring: stages x boxes x 4 KB, 1 KB aligned][mbar][tmem slot]
+    // [slice buffers][ring: stages x boxes x 4 KB, 1 KB aligned][mbarriers][tmem slot][abort]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tile_a = blockIdx.y / tilesB, tile_b = blockIdx.y % tilesB;
     const int a0 = tile_a * BA, b0 = tile_b * BB;
@@ -354,23 +374,38 @@ __global__ void __launch_bounds__(kT5Threads, 1)
     const int nbr2 = r2end > r2beg ? (r2end - r2beg + kT5mBox - 1) / kT5mBox : 0;
     const int c2 = r2beg - kb1;  // first R2 column of this tile's boxes
     const int nbox = nbl + nbr1 + nbr2;
-    const unsigned ring_off = (2 * buf_bytes + 1023) / 1024 * 1024;
+    const unsigned ring_off = (kT5wNB * buf_bytes + 1023) / 1024 * 1024;
     unsigned char *ring = smem_raw + ring_off;
     const unsigned stage_bytes = (unsigned)nbox * kT5mBoxBytes;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(ring + (size_t)stages * stage_bytes);
-    uint64_t *full = mbar + 2;  // one per ring stage
-    unsigned *tmem_slot = reinterpret_cast<unsigned *>(full + stages);
+    uint64_t *full = reinterpret_cast<uint64_t *>(ring + (size_t)stages * stage_bytes);
+    uint64_t *empty = full + stages;
+    uint64_t *sfull = empty + stages;
+    uint64_t *sfree = sfull + kT5wNB;
+    uint64_t *gdone = sfree + kT5wNB;
+    uint64_t *gfree = gdone + 2;
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(gfree + 2);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int64_t rbeg = (int64_t)blockIdx.x * rows_per_chunk;
     const int64_t rend = min(n, rbeg + rows_per_chunk);
     const int64_t nsteps = rend > rbeg ? (rend - rbeg + kT5KT - 1) / kT5KT : 0;
 
-    for (unsigned i = tid; i < 2 * buf_bytes / 16; i += kT5Threads)
+    for (unsigned i = tid; i < kT5wNB * buf_bytes / 16; i += kT5wThreads)
         reinterpret_cast<uint4 *>(smem_raw)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
-        t5_mbar_init(&mbar[0], 1);
-        t5_mbar_init(&mbar[1], 1);
-        for (int q = 0; q < stages; ++q) t5_mbar_init(&full[q], 1);
+        for (int q = 0; q < stages; ++q) {
+            t5_mbar_init(&full[q], 1);
+            t5_mbar_init(&empty[q], kT5wConvWarps);
+        }
+        for (int b = 0; b < kT5wNB; ++b) {
+            t5_mbar_init(&sfull[b], kT5wConvWarps);
+            t5_mbar_init(&sfree[b], 1);
+        }
+        for (int x = 0; x < 2; ++x) {
+            t5_mbar_init(&gdone[x], 1);
+            t5_mbar_init(&gfree[x], kT5wConvWarps);
+        }
+        *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     if (warp == 0) {
@@ -384,199 +419,218 @@ __global__ void __launch_bounds__(kT5Threads, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const unsigned tmem = *tmem_slot;
-
-    // ---- TMA loads of one step (thread 0): the tile's L, R1, R2 boxes
-    int64_t issued = 0;  // steps whose loads were issued (thread 0)
-    auto issue_loads = [&](int64_t j) {
-        if (j >= nsteps) return;
-        const int q = (int)(j % stages);
-        unsigned char *dst = ring + (size_t)q * stage_bytes;
-        const int row0 = (int)(rbeg + j * kT5KT);
-        tma_expect_tx(&full[q], stage_bytes);
-        for (int b = 0; b < nbl; ++b)
-            tma_load_2d(dst + b * kT5mBoxBytes, &tmL, a0 + kT5mBox * b, row0, &full[q]);
-        for (int b = 0; b < nbr1; ++b)
-            tma_load_2d(dst + (nbl + b) * kT5mBoxBytes, &tmR1, b0 + kT5mBox * b, row0, &full[q]);
-        for (int b = 0; b < nbr2; ++b)
-            tma_load_2d(dst + (nbl + nbr1 + b) * kT5mBoxBytes, &tmR2, c2 + kT5mBox * b, row0,
-                        &full[q]);
-        issued = j + 1;
-    };
-
-    // ---- conversion units: (row k of the step, 8-column octet o)
-    int usrc[kT5MaxUnits], uch[kT5MaxUnits], udst[kT5MaxUnits], uslice[kT5MaxUnits], urow[kT5MaxUnits];
-    const int noct = (BA + BB) / 8;
-#pragma unroll
-    for (int u = 0; u < kT5MaxUnits; ++u) {
-        const int id = tid + u * kT5Threads;
-        usrc[u] = -1;
-        uch[u] = 0;
-        udst[u] = 0;
-        uslice[u] = 0;
-        urow[u] = 0;
-        if (id < kT5KT * noct) {
-            const int k = id % kT5KT, o = id / kT5KT;
-            int box, col;  // box of the stage, column of the octet in the box
-            if (o < BA / 8) {
-                box = (8 * o) / kT5mBox;
-                col = (8 * o) % kT5mBox;
-                udst[u] = o * 128 + (k / 8) * (int)lbo_a + (k % 8) * 16;
-                uslice[u] = (int)a_bytes;
-            } else {
-                const int cb = 8 * (o - BA / 8);  // column of the tile's B block
-                if (b0 + cb < kb1) {
-                    box = nbl + cb / kT5mBox;
-                    col = cb % kT5mBox;
-                } else {
-                    const int rel = b0 + cb - kb1 - c2;
-                    box = nbl + nbr1 + rel / kT5mBox;
-                    col = rel % kT5mBox;
-                }
-                udst[u] = 3 * (int)a_bytes + (o - BA / 8) * 128 + (k / 8) * (int)lbo_b + (k % 8) * 16;
-                uslice[u] = (int)b_bytes;
-            }
-            // an octet past the operand's columns (tile wider than the matrix)
-            // has no box: it converts zeros
-            usrc[u] = box < nbox ? box * (int)kT5mBoxBytes + k * 128 : -2;
-            uch[u] = col / 4;  // first of the octet's two 16-byte chunks
-            urow[u] = k;
-        }
-    }
-    auto convert = [&](int64_t j, int buf) {
-        const unsigned char *src = ring + (size_t)(j % stages) * stage_bytes;
-        unsigned char *dbase = smem_raw + buf * buf_bytes;
-        const int64_t r0 = rbeg + j * kT5KT;
-#pragma unroll
-        for (int u = 0; u < kT5MaxUnits; ++u) {
-            if (usrc[u] == -1) continue;
-            const int sw = urow[u] & 7;
-            float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
-            // rows of the next chunk (or past n) and octets without a box stay zero
-            if (usrc[u] >= 0 && r0 + urow[u] < rend) {
-                v0 = *reinterpret_cast<const float4 *>(src + usrc[u] + ((uch[u] ^ sw) << 4));
-                v1 = *reinterpret_cast<const float4 *>(src + usrc[u] + (((uch[u] + 1) ^ sw) << 4));
-            }
-            unsigned hw[4], mw[4], lw[4];
-            t5_split2(v0.x, v0.y, hw[0], mw[0], lw[0]);
-            t5_split2(v0.z, v0.w, hw[1], mw[1], lw[1]);
-            t5_split2(v1.x, v1.y, hw[2], mw[2], lw[2]);
-            t5_split2(v1.z, v1.w, hw[3], mw[3], lw[3]);
-            unsigned char *d = dbase + udst[u];
-            *reinterpret_cast<uint4 *>(d) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-            *reinterpret_cast<uint4 *>(d + uslice[u]) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
-            *reinterpret_cast<uint4 *>(d + 2 * uslice[u]) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-        }
-    };
-
-    // ---- float-float accumulator row of this thread (as gram_tc5_kernel)
-    const int quad = warp & 3, half = warp >> 2;
-    const int row_t = 32 * quad + lane;
-    float acc_hi[HC], acc_lo[HC];
-#pragma unroll
-    for (int q = 0; q < HC; ++q) acc_hi[q] = acc_lo[q] = 0.f;
-    auto flush = [&](int64_t step) {
-        const unsigned tb = (unsigned)(((step / kT5Flush) & 1) * tmem_half);
-#pragma unroll
-        for (int c8 = 0; c8 < NC8; ++c8) {
-            float v[8];
-            t5_ld8(tmem + ((unsigned)(32 * quad) << 16) + tb + (unsigned)(half * HC + 8 * c8), v);
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                float &hi = acc_hi[8 * c8 + q];
-                const float s = hi + v[q];
-                const float bp = s - hi;
-                acc_lo[8 * c8 + q] += (hi - (s - bp)) + (v[q] - bp);
-                hi = s;
-            }
-        }
+    auto fail = [&]() {
+        *abort_flag = 1;
+        atomicOr(status, kStatusTimeout);
     };
     auto group_end = [&](int64_t e) { return e % kT5Flush == kT5Flush - 1 || e == nsteps - 1; };
 
-    const unsigned idesc = t5_idesc(kT5M, BB) | (1u << 15) | (1u << 16);  // A, B MN-major
-    auto issue_mma = [&](int64_t j) {  // thread 0: the 12 MMAs of step j
-        const int buf = (int)(j & 1);
-        const unsigned abase = t5_smem_u32(smem_raw + buf * buf_bytes);
-        const unsigned bbase = abase + 3 * a_bytes;
-        const unsigned d = tmem + (unsigned)(((j / kT5Flush) & 1) * tmem_half);
-        unsigned accumulate = (j % kT5Flush) != 0;
-        const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+    float acc_hi[HC], acc_lo[HC];
 #pragma unroll
-        for (int pr = 0; pr < 6; ++pr) {
-#pragma unroll
-            for (int kk = 0; kk < kT5KT / 16; ++kk) {
-                const uint64_t ad = t5_desc_lbo(abase + pa[pr] * a_bytes + 2 * kk * lbo_a, lbo_a, 128);
-                const uint64_t bd = t5_desc_lbo(bbase + pb[pr] * b_bytes + 2 * kk * lbo_b, lbo_b, 128);
-                t5_mma(d, ad, bd, idesc, accumulate);
-                accumulate = 1;
-            }
-        }
-        t5_commit(&mbar[buf]);
-    };
+    for (int q = 0; q < HC; ++q) acc_hi[q] = acc_lo[q] = 0.f;
 
-    int timed_out = 0, aborted = 0;
-    int64_t last_committed = -1;  // thread 0
-    if (tid == 0)
-        for (int j = 0; j < stages - 1; ++j) issue_loads(j);
-    for (int64_t i = 0; i <= nsteps; ++i) {
-        if (i < nsteps && !timed_out &&
-            !t5_mbar_wait(&full[i % stages], (unsigned)((i / stages) & 1))) {
-            if (lane == 0) atomicOr(status, kStatusTimeout);
-            timed_out = 1;
-        }
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        aborted = __syncthreads_or(timed_out);
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        if (aborted) break;
-        if (i >= 1 && tid == 0) {
-            issue_mma(i - 1);
-            last_committed = i - 1;
-        }
-        if (i == nsteps) break;
-        if (tid == 0) issue_loads(i + stages - 1);  // the stage of step i-1, read before the barrier
-        if (i >= 2) {
-            if (!__all_sync(0xffffffffu, t5_mbar_wait(&mbar[i & 1], (unsigned)(((i - 2) >> 1) & 1)))) {
-                if (lane == 0) atomicOr(status, kStatusTimeout);
-                timed_out = 1;
-            } else {
-                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                if (group_end(i - 2)) flush(i - 2);
+    if (warp < kT5wConvWarps) {
+        // ------------------------------------------------------ converters
+        int usrc[kT5wUnits], uch[kT5wUnits], udst[kT5wUnits], uslice[kT5wUnits], urow[kT5wUnits];
+        const int noct = (BA + BB) / 8;
+#pragma unroll
+        for (int u = 0; u < kT5wUnits; ++u) {
+            const int id = tid + u * kT5wConv;
+            usrc[u] = -1;
+            uch[u] = 0;
+            udst[u] = 0;
+            uslice[u] = 0;
+            urow[u] = 0;
+            if (id < kT5KT * noct) {
+                const int k = id % kT5KT, o = id / kT5KT;
+                int box, col;
+                if (o < BA / 8) {
+                    box = (8 * o) / kT5mBox;
+                    col = (8 * o) % kT5mBox;
+                    udst[u] = o * 128 + (k / 8) * (int)lbo_a + (k % 8) * 16;
+                    uslice[u] = (int)a_bytes;
+                } else {
+                    const int cb = 8 * (o - BA / 8);
+                    if (b0 + cb < kb1) {
+                        box = nbl + cb / kT5mBox;
+                        col = cb % kT5mBox;
+                    } else {
+                        const int rel = b0 + cb - kb1 - c2;
+                        box = nbl + nbr1 + rel / kT5mBox;
+                        col = rel % kT5mBox;
+                    }
+                    udst[u] = 3 * (int)a_bytes + (o - BA / 8) * 128 + (k / 8) * (int)lbo_b +
+                              (k % 8) * 16;
+                    uslice[u] = (int)b_bytes;
+                }
+                // an octet past the operand's columns has no box: it converts zeros
+                usrc[u] = box < nbox ? box * (int)kT5mBoxBytes + k * 128 : -2;
+                uch[u] = col / 4;
+                urow[u] = k;
             }
         }
-        convert(i, (int)(i & 1));
-    }
-    bool ok = !aborted;
-    if (!aborted && nsteps > 0) {
-        const int64_t last = nsteps - 1;
-        ok = __all_sync(0xffffffffu, t5_mbar_wait(&mbar[last & 1], (unsigned)((last >> 1) & 1)));
-        if (!ok && lane == 0) atomicOr(status, kStatusTimeout);
-    } else if (aborted && tid == 0) {
-        // bounded waits for the MMAs and the loads still in flight
-        if (last_committed >= 0)
-            t5_mbar_wait(&mbar[last_committed & 1], (unsigned)((last_committed >> 1) & 1));
-        for (int64_t j = 0; j < issued; ++j)
-            if (j >= issued - stages) t5_mbar_wait(&full[j % stages], (unsigned)((j / stages) & 1));
-    }
-    if (nsteps > 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        if (!aborted) {
-            if (ok && nsteps >= 2 && group_end(nsteps - 2)) flush(nsteps - 2);
-            if (ok) flush(nsteps - 1);
+        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its lane quadrant),
+        // columns [(w / 4) HC, + HC)
+        const int quad = warp & 3, quarter = warp >> 2;
+        auto flush = [&](int64_t step) {
+            const unsigned tb = (unsigned)(((step / kT5Flush) & 1) * tmem_half);
+#pragma unroll
+            for (int c4 = 0; c4 < NC8; ++c4) {
+                float v[4];
+                t5_ld4(tmem + ((unsigned)(32 * quad) << 16) + tb + (unsigned)(quarter * HC + 4 * c4),
+                       v);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float &hi = acc_hi[4 * c4 + q];
+                    const float s = hi + v[q];
+                    const float bp = s - hi;
+                    acc_lo[4 * c4 + q] += (hi - (s - bp)) + (v[q] - bp);
+                    hi = s;
+                }
+            }
+        };
+        // flush of the group ending at step e; false if its MMAs never completed
+        auto flush_group = [&](int64_t e) {
+            const int64_t g = e / kT5Flush;
+            const bool ok = __all_sync(0xffffffffu, t5_mbar_wait_or_abort(
+                                                        &gdone[g & 1], (unsigned)((g >> 1) & 1),
+                                                        abort_flag));
+            if (!ok) return false;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            flush(e);
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) t5_mbar_arrive(&gfree[g & 1]);
+            return true;
+        };
+        bool ok = true;
+        for (int64_t j = 0; j < nsteps && ok; ++j) {
+            const int q = (int)(j % stages), b = (int)(j % kT5wNB);
+            bool w = t5_mbar_wait_or_abort(&full[q], (unsigned)((j / stages) & 1), abort_flag);
+            if (w && j >= kT5wNB)
+                w = t5_mbar_wait_or_abort(&sfree[b], (unsigned)(((j / kT5wNB) - 1) & 1), abort_flag);
+            if (!__all_sync(0xffffffffu, w)) {
+                ok = false;
+                break;
+            }
+            const unsigned char *src = ring + (size_t)q * stage_bytes;
+            unsigned char *dbase = smem_raw + b * buf_bytes;
+            const int64_t r0 = rbeg + j * kT5KT;
+#pragma unroll
+            for (int u = 0; u < kT5wUnits; ++u) {
+                if (usrc[u] == -1) continue;
+                const int sw = urow[u] & 7;
+                float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+                if (usrc[u] >= 0 && r0 + urow[u] < rend) {
+                    v0 = *reinterpret_cast<const float4 *>(src + usrc[u] + ((uch[u] ^ sw) << 4));
+                    v1 = *reinterpret_cast<const float4 *>(src + usrc[u] +
+                                                           (((uch[u] + 1) ^ sw) << 4));
+                }
+                unsigned hw[4], mw[4], lw[4];
+                t5_split2(v0.x, v0.y, hw[0], mw[0], lw[0]);
+                t5_split2(v0.z, v0.w, hw[1], mw[1], lw[1]);
+                t5_split2(v1.x, v1.y, hw[2], mw[2], lw[2]);
+                t5_split2(v1.z, v1.w, hw[3], mw[3], lw[3]);
+                unsigned char *d = dbase + udst[u];
+                *reinterpret_cast<uint4 *>(d) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(d + uslice[u]) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+                *reinterpret_cast<uint4 *>(d + 2 * uslice[u]) =
+                    make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+            // slices visible to the tensor cores; the stage may be refilled
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) {
+                t5_mbar_arrive(&sfull[b]);
+                t5_mbar_arrive(&empty[q]);
+            }
+            if (j >= 2 && group_end(j - 2)) ok = flush_group(j - 2);
         }
+        // the last groups' sums
+        for (int64_t e = nsteps - 2; ok && e < nsteps; ++e)
+            if (e >= 0 && group_end(e)) ok = flush_group(e);
+        if (!ok && lane == 0) fail();
+    } else if (tid == kT5wConv) {
+        // ---------------------------------------------------------- loader
+        int64_t issued = 0;
+        for (int64_t j = 0; j < nsteps; ++j) {
+            const int q = (int)(j % stages);
+            if (j >= stages &&
+                !t5_mbar_wait_or_abort(&empty[q], (unsigned)(((j / stages) - 1) & 1), abort_flag)) {
+                fail();
+                break;
+            }
+            unsigned char *dst = ring + (size_t)q * stage_bytes;
+            const int row0 = (int)(rbeg + j * kT5KT);
+            tma_expect_tx(&full[q], stage_bytes);
+            for (int bx = 0; bx < nbl; ++bx)
+                tma_load_2d(dst + bx * kT5mBoxBytes, &tmL, a0 + kT5mBox * bx, row0, &full[q]);
+            for (int bx = 0; bx < nbr1; ++bx)
+                tma_load_2d(dst + (nbl + bx) * kT5mBoxBytes, &tmR1, b0 + kT5mBox * bx, row0,
+                            &full[q]);
+            for (int bx = 0; bx < nbr2; ++bx)
+                tma_load_2d(dst + (nbl + nbr1 + bx) * kT5mBoxBytes, &tmR2, c2 + kT5mBox * bx, row0,
+                            &full[q]);
+            issued = j + 1;
+        }
+        if (*abort_flag)  // let the loads in flight land (bounded)
+            for (int64_t j = issued - stages > 0 ? issued - stages : 0; j < issued; ++j)
+                t5_mbar_wait(&full[j % stages], (unsigned)((j / stages) & 1));
+    } else if (tid == kT5wConv + 32) {
+        // ---------------------------------------------------- MMA issuer
+        const unsigned idesc = t5_idesc(kT5M, BB) | (1u << 15) | (1u << 16);  // A, B MN-major
+        int64_t last = -1;
+        for (int64_t j = 0; j < nsteps; ++j) {
+            const int b = (int)(j % kT5wNB);
+            const int64_t g = j / kT5Flush;
+            if (!t5_mbar_wait_or_abort(&sfull[b], (unsigned)((j / kT5wNB) & 1), abort_flag) ||
+                (j % kT5Flush == 0 && g >= 2 &&
+                 !t5_mbar_wait_or_abort(&gfree[g & 1], (unsigned)(((g >> 1) - 1) & 1),
+                                        abort_flag))) {
+                fail();
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const unsigned abase = t5_smem_u32(smem_raw + b * buf_bytes);
+            const unsigned bbase = abase + 3 * a_bytes;
+            const unsigned dt = tmem + (unsigned)((g & 1) * tmem_half);
+            unsigned accumulate = (j % kT5Flush) != 0;
+            const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+            for (int pr = 0; pr < 6; ++pr) {
+#pragma unroll
+                for (int kk = 0; kk < kT5KT / 16; ++kk) {
+                    const uint64_t ad =
+                        t5_desc_lbo(abase + pa[pr] * a_bytes + 2 * kk * lbo_a, lbo_a, 128);
+                    const uint64_t bd =
+                        t5_desc_lbo(bbase + pb[pr] * b_bytes + 2 * kk * lbo_b, lbo_b, 128);
+                    t5_mma(dt, ad, bd, idesc, accumulate);
+                    accumulate = 1;
+                }
+            }
+            t5_commit(&sfree[b]);
+            if (group_end(j)) t5_commit(&gdone[g & 1]);
+            last = j;
+        }
+        if (*abort_flag && last >= 0)  // the committed MMAs finish before TMEM goes (bounded)
+            t5_mbar_wait(&sfree[last % kT5wNB], (unsigned)((last / kT5wNB) & 1));
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    const int bad = __syncthreads_or(!ok);
+    const int bad = __syncthreads_or(*abort_flag);
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
                      "r"(2 * tmem_half));
     }
-    if (bad || row_t >= BA) return;
+    if (bad || warp >= kT5wConvWarps) return;
+    const int row_t = 32 * (warp & 3) + lane, quarter = warp >> 2;
+    if (row_t >= BA) return;
     double *out = part + ((size_t)blockIdx.x * gridDim.y + blockIdx.y) * (size_t)BA * BB +
-                  (size_t)row_t * BB + half * HC;
+                  (size_t)row_t * BB + quarter * HC;
 #pragma unroll
     for (int q = 0; q < HC; ++q) out[q] = (double)acc_hi[q] + (double)acc_lo[q];
 }
+
 
 struct T5Plan {
     int BA, BB, tilesA, tilesB, nchunks, tmem_half;
@@ -669,12 +723,13 @@ static int launch_tc5m(cudaStream_t st, const T5Plan &p, int64_t n, const float 
         tmR2 = tmR1;  // never loaded
     }
     const size_t buf = 3 * ((size_t)kT5M * kT5KT * 2 + (size_t)p.BB * kT5KT * 2);
-    const size_t ring_off = (2 * buf + 1023) / 1024 * 1024;
+    const size_t ring_off = (kT5wNB * buf + 1023) / 1024 * 1024;
     const int nbox_max = (p.BA + kT5mBox - 1) / kT5mBox + (p.BB + kT5mBox - 1) / kT5mBox + 1;
     int stages = 4;
     size_t smem = 0;
     for (; stages >= 2; --stages) {
-        smem = ring_off + (size_t)stages * nbox_max * kT5mBoxBytes + (2 + stages) * 8 + 16;
+        smem = ring_off + (size_t)stages * nbox_max * kT5mBoxBytes +
+               (2 * stages + 2 * kT5wNB + 4) * 8 + 16;
         if (smem <= max_smem_optin()) break;
     }
     if (stages < 2) return CACG_ERR_UNSUPPORTED;
@@ -682,7 +737,7 @@ static int launch_tc5m(cudaStream_t st, const T5Plan &p, int64_t n, const float 
 #define T5M_CASE(NC)                                                                               \
     case NC:                                                                                       \
         t5m_set_attr<NC>();                                                                        \
-        gram_tc5m_kernel<NC><<<grid, kT5Threads, smem, st>>>(tmL, tmR1, tmR2, n, p.rows_per_chunk, \
+        gram_tc5m_kernel<NC><<<grid, kT5wThreads, smem, st>>>(tmL, tmR1, tmR2, n, p.rows_per_chunk, \
                                                              ka, kb1, kb2, p.BA, p.tilesB,         \
                                                              p.tmem_half, stages, ws, status);     \
         break;
