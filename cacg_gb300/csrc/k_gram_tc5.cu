@@ -472,20 +472,29 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
         // warp w reads TMEM lanes 32 (w % 4) .. + 31 (its lane quadrant),
         // columns [(w / 4) HC, + HC)
         const int quad = warp & 3, quarter = warp >> 2;
+        // TMEM loads of up to 16 columns go out together, then one wait
         auto flush = [&](int64_t step) {
             const unsigned tb = (unsigned)(((step / kT5Flush) & 1) * tmem_half);
+            const unsigned ta = tmem + ((unsigned)(32 * quad) << 16) + tb + (unsigned)(quarter * HC);
 #pragma unroll
-            for (int c4 = 0; c4 < NC8; ++c4) {
-                float v[4];
-                t5_ld4(tmem + ((unsigned)(32 * quad) << 16) + tb + (unsigned)(quarter * HC + 4 * c4),
-                       v);
+            for (int h0 = 0; h0 < NC8; h0 += 4) {
+                unsigned r[4][4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    float &hi = acc_hi[4 * c4 + q];
-                    const float s = hi + v[q];
-                    const float bp = s - hi;
-                    acc_lo[4 * c4 + q] += (hi - (s - bp)) + (v[q] - bp);
-                    hi = s;
+                for (int c4 = 0; c4 < 4; ++c4)
+                    if (h0 + c4 < NC8) t5_ld4_nowait(ta + 4 * (h0 + c4), r[c4]);
+                t5_wait_ld();
+#pragma unroll
+                for (int c4 = 0; c4 < 4; ++c4) {
+                    if (h0 + c4 >= NC8) break;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const float v = __uint_as_float(r[c4][q]);
+                        float &hi = acc_hi[4 * (h0 + c4) + q];
+                        const float s = hi + v;
+                        const float bp = s - hi;
+                        acc_lo[4 * (h0 + c4) + q] += (hi - (s - bp)) + (v - bp);
+                        hi = s;
+                    }
                 }
             }
         };

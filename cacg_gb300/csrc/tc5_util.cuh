@@ -135,6 +135,17 @@ __device__ __forceinline__ void t5_ld4(unsigned taddr, float (&v)[4]) {
     for (int q = 0; q < 4; ++q) v[q] = __uint_as_float(r[q]);
 }
 
+// the same load without the wait: several can be in flight before one
+// t5_wait_ld(); the registers are valid only after it
+__device__ __forceinline__ void t5_ld4_nowait(unsigned taddr, unsigned (&r)[4]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void t5_wait_ld() {
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
 __device__ __forceinline__ void t5_fence_before() {
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
 }
