@@ -28,7 +28,13 @@ __device__ __forceinline__ void ff_split_bits(double x, float &hi, float &lo) {
     // rem * 2^(e - 1075): the scale is a normal FP32 power of two in this range
     const int se = e - 1075 + 127;
     const float scale = se >= 1 ? __uint_as_float((unsigned)se << 23) : 0.f;
-    const float l = __uint2float_rn(rem) * scale;
+    // (float)rem, rounded to nearest, without an integer conversion (which
+    // runs on the slow conversion pipe here): each 16-bit half is exact as
+    // (2^23 + half) - 2^23, the high half times 2^16 stays exact, and the one
+    // addition rounds like the conversion would
+    const float rh = __fsub_rn(__uint_as_float(0x4B000000u | (rem >> 16)), 8388608.f);
+    const float rl = __fsub_rn(__uint_as_float(0x4B000000u | (rem & 0xFFFFu)), 8388608.f);
+    const float l = __fadd_rn(__fmul_rn(rh, 65536.f), rl) * scale;
     lo = sgn ? -l : l;
 }
 
