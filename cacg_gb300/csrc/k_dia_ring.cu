@@ -15,7 +15,11 @@
 // TMA load per chunk, and the FMAs read it from shared memory.  The block's
 // DIA values (ndiag x BR FP32) come by one more TMA load into a double buffer.
 //
-// Threads.  128 threads; thread (lr, c) = (tid / 4, tid % 4) computes rows
+// Threads.  128 compute threads and a producer warp (one thread issues the
+// TMA loads); the producer refills block u - 1's slot and value buffer as
+// soon as the four compute warps have arrived on that block's "done"
+// mbarrier, so the warps run independently (no CTA-wide barrier per block).
+// Thread (lr, c) = (tid / 4, tid % 4) computes rows
 // r0 + 3 lr + i (i < 3) of columns 4c .. 4c + 3.  Three rows per thread (an
 // odd count) puts the two rows that a quarter warp's 16-byte loads touch in
 // 64-byte slots of different parity, i.e. on disjoint banks.  Each output
@@ -130,7 +134,7 @@ __device__ __forceinline__ void ring_group(const unsigned char *ring, int q, con
 // 3 x 3 x 3), loops unrolled so the window loads of later groups can be
 // issued ahead of earlier groups' FMAs; NB = 0: any layout, read from rd.
 template <int NB, int GPB, int G>
-__global__ void __launch_bounds__(kRingThreads, 2)
+__global__ void __launch_bounds__(kRingThreads + 32, 2)
     dia_ring_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmm,
                     const __grid_constant__ CUtensorMap tmv,
                     int64_t n, int64_t nitems, const DiaDesc desc, const __grid_constant__ RingDesc rd,
@@ -138,20 +142,70 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                     const float *__restrict__ Z2, int64_t ldz2, float ca, float cb, float cc,
                     int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char ring_smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(ring_smem + rd.boff);
+    // full[2]: block u's loads landed (TMA); done[2]: the four compute warps
+    // finished block u (its ring slots and value buffer may be refilled)
+    uint64_t *full = reinterpret_cast<uint64_t *>(ring_smem + rd.boff);
+    uint64_t *done = full + 2;
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(done + 2);
     const int tid = threadIdx.x, lr = tid / kRingCpr, c = tid % kRingCpr;
     const int rowoff = lr * kRingR;
     if (tid == 0) {
-        t5_mbar_init(&bar[0], 1);
-        t5_mbar_init(&bar[1], 1);
+        t5_mbar_init(&full[0], 1);
+        t5_mbar_init(&full[1], 1);
+        t5_mbar_init(&done[0], kRingThreads / 32);
+        t5_mbar_init(&done[1], kRingThreads / 32);
+        *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         t5_fence_proxy_async();
     }
     __syncthreads();
 
     const int64_t nblk = (n + kRingBR - 1) / kRingBR;
-    unsigned u = 0;       // blocks this CTA has computed (barrier stage and parity)
-    unsigned issued = 0;  // blocks whose loads are issued (thread 0)
+    if (tid >= kRingThreads) {
+        // ------------------------------------------------ producer (one thread)
+        if (tid != kRingThreads) return;
+        unsigned u = 0, issued = 0;
+        bool stop = false;
+        // false (and the abort flag set) if block v did not finish in time
+        auto wait_done = [&](unsigned v) {
+            if (t5_mbar_wait_or_abort(&done[v & 1], (v >> 1) & 1, abort_flag)) return true;
+            if (!*abort_flag) atomicOr(status, kStatusTimeout);
+            *abort_flag = 1;
+            return false;
+        };
+        for (int64_t it = blockIdx.x; it < nitems && !stop; it += gridDim.x) {
+            const int64_t ri = it / rd.tiles;
+            const int col0 = (int)(it % rd.tiles) * kRingCols;
+            const int64_t b0 = ri * rd.sb;
+            const int nbk = (int)std::min<int64_t>(rd.sb, nblk - b0);
+            const int64_t R0 = b0 * kRingBR;
+            // the item's start-up chunks take every slot: block u - 1 must be done
+            if (u >= 1 && !wait_done(u - 1)) break;
+            t5_fence_proxy_async();
+            ring_issue(ring_smem, rd, &tmx, &tmm, &tmv, R0, col0, 0, true,
+                       ring_smem + rd.voff + (u & 1) * rd.vbytes, &full[u & 1]);
+            ++issued;
+            for (int t = 0; t < nbk; ++t, ++u) {
+                if (t + 1 >= nbk) continue;
+                // block t + 1 takes the slot of block t - 1's first chunk and the
+                // value buffer of block t - 1 (t = 0: waited for above)
+                if (t >= 1 && !wait_done(u - 1)) {
+                    stop = true;
+                    break;
+                }
+                t5_fence_proxy_async();
+                ring_issue(ring_smem, rd, &tmx, &tmm, &tmv, R0, col0, t + 1, false,
+                           ring_smem + rd.voff + ((u + 1) & 1) * rd.vbytes, &full[(u + 1) & 1]);
+                ++issued;
+            }
+        }
+        if (*abort_flag)  // let the loads in flight land before the CTA exits (bounded)
+            for (unsigned v = issued >= 2 ? issued - 2 : 0; v < issued; ++v)
+                t5_mbar_wait(&full[v & 1], (v >> 1) & 1);
+        return;
+    }
+    // ------------------------------------------------------ compute warps
+    unsigned u = 0;  // blocks computed (barrier stage and parity)
     bool timeout = false;
     for (int64_t it = blockIdx.x; it < nitems && !timeout; it += gridDim.x) {
         const int64_t ri = it / rd.tiles;
@@ -162,27 +216,7 @@ __global__ void __launch_bounds__(kRingThreads, 2)
         int base[kRingBandMax];  // ring row of the block's first row, band b: t BR mod cap
 #pragma unroll
         for (int b = 0; b < kRingBandMax; ++b) base[b] = 0;
-        if (tid == 0) {
-            // the previous item's blocks are done (barrier at the end of each block)
-            t5_fence_proxy_async();
-            ring_issue(ring_smem, rd, &tmx, &tmm, &tmv, R0, col0, 0, true,
-                       ring_smem + rd.voff + (u & 1) * rd.vbytes, &bar[u & 1]);
-            ++issued;
-            if (nbk > 1) {
-                ring_issue(ring_smem, rd, &tmx, &tmm, &tmv, R0, col0, 1, false,
-                           ring_smem + rd.voff + ((u + 1) & 1) * rd.vbytes, &bar[(u + 1) & 1]);
-                ++issued;
-            }
-        }
         for (int t = 0; t < nbk; ++t, ++u) {
-            if (tid == 0 && t >= 1 && t + 1 < nbk) {
-                // block t + 1 takes the slot of block t - 1's first chunk and the
-                // value buffer of block t - 1, both released by the last barrier
-                t5_fence_proxy_async();
-                ring_issue(ring_smem, rd, &tmx, &tmm, &tmv, R0, col0, t + 1, false,
-                           ring_smem + rd.voff + ((u + 1) & 1) * rd.vbytes, &bar[(u + 1) & 1]);
-                ++issued;
-            }
             // the recurrence operands from global memory do not wait for the
             // staged rows: their loads go out before the barrier wait
             const int64_t rbase = R0 + (int64_t)t * kRingBR + rowoff;
@@ -197,8 +231,13 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                 z2v[i] = Z2 && in ? *reinterpret_cast<const float4 *>(Z2 + (rbase + i) * ldz2 + col)
                                   : make_float4(0.f, 0.f, 0.f, 0.f);
             }
-            const bool ok = t5_mbar_wait(&bar[u & 1], (u >> 1) & 1);
-            if (__syncthreads_or(!ok)) {
+            const bool ok = __all_sync(0xffffffffu, t5_mbar_wait_or_abort(
+                                                        &full[u & 1], (u >> 1) & 1, abort_flag));
+            if (!ok) {
+                if ((tid & 31) == 0) {
+                    if (!*abort_flag) atomicOr(status, kStatusTimeout);
+                    *abort_flag = 1;
+                }
                 timeout = true;
                 break;
             }
@@ -276,13 +315,10 @@ __global__ void __launch_bounds__(kRingThreads, 2)
                     if (base[b] >= rd.cap[b]) base[b] -= rd.cap[b];
                 }
             }
-            __syncthreads();  // ring slot of this block's first chunk and its values are free
+            // this warp is done with the block's ring slots and values
+            __syncwarp();
+            if ((tid & 31) == 0) t5_mbar_arrive(&done[u & 1]);
         }
-    }
-    if (timeout && tid == 0) {
-        atomicOr(status, kStatusTimeout);
-        // let the loads in flight land before the CTA's shared memory goes away
-        for (unsigned v = u; v < issued; ++v) t5_mbar_wait(&bar[v & 1], (v >> 1) & 1);
     }
 }
 
@@ -331,7 +367,7 @@ bool ring_plan(const DiaDesc &D, RingDesc *rd, size_t *smem) {
     rd->vbytes = (rd->vtx + 127) / 128 * 128;
     off += 2 * (size_t)rd->vbytes;
     rd->boff = (int)off;
-    off += 16;
+    off += 48;  // full[2], done[2], abort flag
     *smem = off;
     return off <= (size_t)kRingSmemMax;
 }
@@ -349,7 +385,7 @@ int ring_launch(cudaStream_t st, const CUtensorMap &tmx, const CUtensorMap &tmm,
     (void)attr;
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dia_ring_kernel<NB, GPB, G>,
-                                                      kRingThreads, smem) != cudaSuccess ||
+                                                      kRingThreads + 32, smem) != cudaSuccess ||
         occ < 1) {
         cudaGetLastError();
         return CACG_ERR_UNSUPPORTED;
@@ -363,7 +399,7 @@ int ring_launch(cudaStream_t st, const CUtensorMap &tmx, const CUtensorMap &tmm,
     rd.sb = (int)std::max<int64_t>(2 * kmax, (nblk + want - 1) / want);
     const int64_t nitems = (nblk + rd.sb - 1) / rd.sb * rd.tiles;
     const int64_t grid = std::min<int64_t>(grid0, nitems);
-    dia_ring_kernel<NB, GPB, G><<<(unsigned)grid, kRingThreads, smem, st>>>(
+    dia_ring_kernel<NB, GPB, G><<<(unsigned)grid, kRingThreads + 32, smem, st>>>(
         tmx, tmm, tmv, n, nitems, desc, rd, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc, status);
     return check_launch();
 }
