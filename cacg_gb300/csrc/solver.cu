@@ -543,6 +543,8 @@ struct Solver {
                     int rc = launch_dia_ring(st, A, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb,
                                              cc, b.status);
                     if (rc != CACG_ERR_UNSUPPORTED) return rc;
+                    rc = launch_dia_wide(st, A, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc);
+                    if (rc != CACG_ERR_UNSUPPORTED) return rc;
                 }
             }
             int rc = launch_dia_spmm<T>(st, A, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb, cc);
