@@ -187,10 +187,11 @@ int launch_gram_tc5(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int
                     size_t ws_bytes, int *status);
 size_t gram_tc5_workspace_bytes(int64_t n, int ka, int kb);
 bool gram_tc5_supported(int ka, int kb);
-// Q_out = S - Q_in beta on tcgen05 (FP32 Q, S; FP64 beta), k % 16 == 0, k <= 96
+// Q_out = S - Q_in beta on tcgen05 (FP32 Q, S; FP64 beta), k % 16 == 0, k <= 96;
+// TMA-fed unless allow_tma is false (then the cp.async-fed kernel, same results)
 int launch_qupdate_tc5(cudaStream_t st, int64_t n, int k, float *Qout, int64_t ldo,
                        const float *Qin, int64_t ldq, const float *S, int64_t lds,
-                       const double *beta, int *status);
+                       const double *beta, int *status, bool allow_tma = true);
 bool tsm_q_tc5_supported(int k);
 // X += Q alpha, R -= AQ alpha, S0 = R32 = (float)R, norms: tcgen05, m <= 16, k <= 256
 int launch_xrupdate_tc5(cudaStream_t st, int64_t n, int k, int m, const float *Q,

@@ -34,6 +34,7 @@
 
 #include "cacg_internal.cuh"
 #include "tc5_util.cuh"
+#include "tma_util.cuh"
 
 namespace cacg {
 
@@ -258,6 +259,326 @@ __global__ void __launch_bounds__(kTsThreads, 1)
             t5_fence_before();
             __syncwarp();
             if (lane == 0) t5_mbar_arrive(&acc_empty[tb]);
+        }
+    }
+    t5_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        t5_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                     "r"(2 * tmem_half));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The same Q update fed by TMA, warp-specialised (operands with 16-byte
+// aligned bases and row strides).  Per tile of 128 rows:
+//   * a loader thread streams the tile's K steps of Q_in (128 rows x 32
+//     columns FP32 boxes, 128-byte swizzle) into a 4-stage ring; a second
+//     loader brings the tile's S (k/32 boxes of 128 x 32) into one staging
+//     buffer as soon as the previous tile's stores have read it;
+//   * 8 converter warps split each ring stage into the three bf16 slices
+//     (K-major core matrices, as tsm_q_tc5_kernel) and release the stage;
+//     the MMA thread issues the step's 12 MMAs into one of two TMEM
+//     accumulators;
+//   * 4 epilogue warps (one per TMEM lane quadrant) subtract the
+//     accumulator from the staged S in place (a thread's row, 16-byte chunks
+//     at swizzled positions: conflict-free) and write their 32 rows with TMA
+//     stores, so every global access is whole 128-byte row pieces.
+// Hand-offs are mbarriers with bounded waits (kStatusTimeout and the abort
+// flag on expiry); no CTA-wide barrier after the setup.  The MMAs and their
+// order are those of tsm_q_tc5_kernel, so the results are bit-identical.
+constexpr int kQwConvWarps = 8;
+constexpr int kQwConv = 32 * kQwConvWarps;       // converter threads (warps 0-7)
+constexpr int kQwEpiWarp0 = kQwConvWarps;        // warps 8-11: epilogue
+constexpr int kQwLoadWarp = kQwEpiWarp0 + 4;     // warp 12: Q_in loader
+constexpr int kQwMmaWarp = kQwLoadWarp + 1;      // warp 13: MMA issuer
+constexpr int kQwSWarp = kQwMmaWarp + 1;         // warp 14: S loader
+constexpr int kQwThreads = 32 * (kQwSWarp + 1);  // 480
+constexpr int kQwStages = 4;
+constexpr unsigned kQwBox = kTsM * kTsKT * 4;    // one 128 x 32 FP32 box (16 KB)
+constexpr int kQwBars = 2 * kQwStages + 10;  // full, empty; sfull, sfree, afull, afree; stfull, stfree
+
+struct QwLayout {
+    unsigned asl, ring, stg, bars, total;
+};
+__host__ __device__ constexpr unsigned qw_align1k(unsigned x) { return (x + 1023u) & ~1023u; }
+// [beta slices 3 x k x Kp bf16][A slices 2 x 3 x 8 KB][ring 4 x 16 KB][S staging
+// Kp/32 x 16 KB][mbarriers][tmem slot][abort]; the ring and the staging 1 KB
+// aligned (128-byte swizzle)
+__host__ __device__ constexpr QwLayout qw_layout(int K) {
+    const unsigned Kp = (unsigned)(K + 31) / 32 * 32;
+    const unsigned asl = qw_align1k(3u * (unsigned)K * Kp * 2u);
+    const unsigned ring = qw_align1k(asl + 2u * 3u * kTsABytes);
+    const unsigned stg = ring + (unsigned)kQwStages * kQwBox;
+    const unsigned bars = stg + Kp / 32u * kQwBox;
+    return QwLayout{asl, ring, stg, bars, bars + 8u * (unsigned)kQwBars + 16u};
+}
+
+template <int NN>
+__global__ void __launch_bounds__(kQwThreads, 1)
+    tsm_q_tc5w_kernel(const __grid_constant__ CUtensorMap tmQ,
+                      const __grid_constant__ CUtensorMap tmS,
+                      const __grid_constant__ CUtensorMap tmO, int64_t n,
+                      const double *__restrict__ beta, int tmem_half, int *__restrict__ status) {
+    constexpr int K = 16 * NN;
+    constexpr int Kp = (K + 31) / 32 * 32;
+    constexpr int KS = Kp / kTsKT;  // steps per tile = S boxes per tile
+    constexpr unsigned w_bytes = K * Kp * 2;
+    constexpr QwLayout L = qw_layout(K);
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *wsl = smem_raw;
+    unsigned char *asl = smem_raw + L.asl;
+    unsigned char *ring = smem_raw + L.ring;
+    unsigned char *stg = smem_raw + L.stg;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + L.bars);
+    uint64_t *empty = full + kQwStages;
+    uint64_t *sfull = empty + kQwStages;  // A slice buffers converted
+    uint64_t *sfree = sfull + 2;          // A slice buffers read by the MMAs
+    uint64_t *afull = sfree + 2;          // accumulators complete
+    uint64_t *afree = afull + 2;          // accumulators read
+    uint64_t *stfull = afree + 2;         // S staging loaded
+    uint64_t *stfree = stfull + 1;        // S staging stored
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(stfree + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t ntiles = (n + kTsM - 1) / kTsM;
+    const int64_t my_tiles =
+        ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t nsteps = my_tiles * KS;
+
+    // beta^T slices (B operand: row c = output column, K-major), zero-padded to Kp
+    for (int pidx = tid; pidx < K * Kp / 2; pidx += kQwThreads) {
+        const int c = pidx / (Kp / 2), j = 2 * (pidx % (Kp / 2));
+        const float w0 = j < K ? (float)beta[(size_t)j * K + c] : 0.f;
+        const float w1 = j + 1 < K ? (float)beta[(size_t)(j + 1) * K + c] : 0.f;
+        unsigned hw, mw, lw;
+        t5_split2(w0, w1, hw, mw, lw);
+        const unsigned off = (((c >> 3) * (Kp / 8) + (j >> 3)) * 64 + (c & 7) * 8 + (j & 7)) * 2;
+        *reinterpret_cast<unsigned *>(wsl + off) = hw;
+        *reinterpret_cast<unsigned *>(wsl + w_bytes + off) = mw;
+        *reinterpret_cast<unsigned *>(wsl + 2 * w_bytes + off) = lw;
+    }
+    if (tid == 0) {
+        for (int q = 0; q < kQwStages; ++q) {
+            t5_mbar_init(&full[q], 1);
+            t5_mbar_init(&empty[q], kQwConvWarps);
+        }
+        for (int b = 0; b < 2; ++b) {
+            t5_mbar_init(&sfull[b], kQwConvWarps);
+            t5_mbar_init(&sfree[b], 1);
+            t5_mbar_init(&afull[b], 1);
+            t5_mbar_init(&afree[b], 4);
+        }
+        t5_mbar_init(stfull, 1);
+        t5_mbar_init(stfree, 4);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         t5_smem_u32(tmem_slot)),
+                     "r"(2 * tmem_half));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    t5_fence_proxy_async();
+    t5_fence_before();
+    __syncthreads();
+    t5_fence_after();
+    const unsigned tmem = *tmem_slot;
+    auto fail = [&]() {
+        *abort_flag = 1;
+        atomicOr(status, kStatusTimeout);
+    };
+    auto tile_row0 = [&](int64_t tj) { return (int)((blockIdx.x + tj * gridDim.x) * kTsM); };
+
+    if (warp < kQwConvWarps) {
+        // ------------------------------------------------------ converters
+        // unit u: row 8g + q8 of the tile, K columns 8o .. 8o + 7 of the step
+        int urow[2], uo[2];
+        unsigned udst[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int id = tid + u * kQwConv;
+            const int q8 = id & 7, o = (id >> 3) & 3, g = id >> 5;
+            urow[u] = 8 * g + q8;
+            uo[u] = o;
+            udst[u] = (unsigned)(((urow[u] >> 3) * (kTsKT / 8) + o) * 128 + (urow[u] & 7) * 16);
+        }
+        bool ok = true;
+        for (int64_t j = 0; j < nsteps; ++j) {
+            const int q = (int)(j % kQwStages), b = (int)(j & 1);
+            bool w = t5_mbar_wait_or_abort(&full[q], (unsigned)((j / kQwStages) & 1), abort_flag);
+            if (w && j >= 2)
+                w = t5_mbar_wait_or_abort(&sfree[b], (unsigned)(((j >> 1) - 1) & 1), abort_flag);
+            if (!__all_sync(0xffffffffu, w)) {
+                ok = false;
+                break;
+            }
+            const unsigned char *src = ring + (size_t)q * kQwBox;
+            unsigned char *dst = asl + b * 3 * kTsABytes;
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int sw = urow[u] & 7;
+                const unsigned char *rp = src + urow[u] * 128;
+                const float4 x0 = *reinterpret_cast<const float4 *>(rp + (((2 * uo[u]) ^ sw) << 4));
+                const float4 x1 =
+                    *reinterpret_cast<const float4 *>(rp + (((2 * uo[u] + 1) ^ sw) << 4));
+                unsigned hw[4], mw[4], lw[4];
+                t5_split2(x0.x, x0.y, hw[0], mw[0], lw[0]);
+                t5_split2(x0.z, x0.w, hw[1], mw[1], lw[1]);
+                t5_split2(x1.x, x1.y, hw[2], mw[2], lw[2]);
+                t5_split2(x1.z, x1.w, hw[3], mw[3], lw[3]);
+                unsigned char *d = dst + udst[u];
+                *reinterpret_cast<uint4 *>(d) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(d + kTsABytes) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+                *reinterpret_cast<uint4 *>(d + 2 * kTsABytes) =
+                    make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+            // slices visible to the tensor cores; the ring stage may be refilled
+            t5_fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) {
+                t5_mbar_arrive(&sfull[b]);
+                t5_mbar_arrive(&empty[q]);
+            }
+        }
+        if (!ok && lane == 0) fail();
+    } else if (warp < kQwLoadWarp) {
+        // -------------------------------------------------------- epilogue
+        const int quad = warp & 3;     // TMEM lanes 32 quad .. + 31
+        const int r = 32 * quad + lane;  // row of the tile
+        bool ok = true;
+        for (int64_t tj = 0; tj < my_tiles; ++tj) {
+            const int tb = (int)(tj & 1);
+            bool w = t5_mbar_wait_or_abort(&afull[tb], (unsigned)((tj >> 1) & 1), abort_flag);
+            if (w) w = t5_mbar_wait_or_abort(stfull, (unsigned)(tj & 1), abort_flag);
+            if (!__all_sync(0xffffffffu, w)) {
+                ok = false;
+                break;
+            }
+            t5_fence_after();
+            const unsigned tbase =
+                tmem + ((unsigned)(32 * quad) << 16) + (unsigned)(tb * tmem_half);
+#pragma unroll
+            for (int c3 = 0; c3 < KS; ++c3) {
+                unsigned char *rowp = stg + c3 * kQwBox + r * 128;
+#pragma unroll
+                for (int c8 = 0; c8 < 4; ++c8) {
+                    if (32 * c3 + 8 * c8 >= K) break;
+                    float v[8];
+                    t5_ld8(tbase + (unsigned)(32 * c3 + 8 * c8), v);
+                    float4 *p0 = reinterpret_cast<float4 *>(rowp + (((2 * c8) ^ (r & 7)) << 4));
+                    float4 *p1 = reinterpret_cast<float4 *>(rowp + (((2 * c8 + 1) ^ (r & 7)) << 4));
+                    const float4 a = *p0, bq = *p1;
+                    *p0 = make_float4(a.x - v[0], a.y - v[1], a.z - v[2], a.w - v[3]);
+                    *p1 = make_float4(bq.x - v[4], bq.y - v[5], bq.z - v[6], bq.w - v[7]);
+                }
+            }
+            // accumulator read: the MMAs may reuse it; rows visible to the TMA store
+            t5_fence_before();
+            t5_fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) {
+                t5_mbar_arrive(&afree[tb]);
+                const int y = tile_row0(tj) + 32 * quad;
+                if (y < n) {  // a quadrant wholly past the last row has nothing to store
+#pragma unroll
+                    for (int c3 = 0; c3 < KS; ++c3)
+                        tma_store_2d(&tmO, 32 * c3, y, stg + c3 * kQwBox + quad * 32 * 128);
+                    tma_store_commit();
+                    tma_store_wait_read();
+                }
+                t5_mbar_arrive(stfree);
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            tma_store_wait_all();
+            if (!ok) fail();
+        }
+    } else if (warp == kQwLoadWarp) {
+        // ---------------------------------------------------- Q_in loader
+        if (lane == 0) {
+            int64_t issued = 0;
+            for (int64_t j = 0; j < nsteps; ++j) {
+                const int q = (int)(j % kQwStages);
+                if (j >= kQwStages &&
+                    !t5_mbar_wait_or_abort(&empty[q], (unsigned)(((j / kQwStages) - 1) & 1),
+                                           abort_flag)) {
+                    fail();
+                    break;
+                }
+                tma_expect_tx(&full[q], kQwBox);
+                tma_load_2d(ring + (size_t)q * kQwBox, &tmQ, (int)(j % KS) * kTsKT,
+                            tile_row0(j / KS), &full[q]);
+                issued = j + 1;
+            }
+            if (*abort_flag)  // the loads in flight land before the CTA exits (bounded)
+                for (int64_t j = issued > kQwStages ? issued - kQwStages : 0; j < issued; ++j)
+                    t5_mbar_wait(&full[j % kQwStages], (unsigned)((j / kQwStages) & 1));
+        }
+    } else if (warp == kQwMmaWarp) {
+        // ---------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            constexpr unsigned idesc = t5_idesc(kTsM, K);
+            int64_t last = -1;
+            for (int64_t j = 0; j < nsteps; ++j) {
+                const int b = (int)(j & 1);
+                const int64_t tj = j / KS;
+                const int kc = (int)(j % KS);
+                const int tb = (int)(tj & 1);
+                if ((kc == 0 && tj >= 2 &&
+                     !t5_mbar_wait_or_abort(&afree[tb], (unsigned)(((tj - 2) >> 1) & 1),
+                                            abort_flag)) ||
+                    !t5_mbar_wait_or_abort(&sfull[b], (unsigned)((j >> 1) & 1), abort_flag)) {
+                    fail();
+                    break;
+                }
+                t5_fence_after();
+                const unsigned d = tmem + (unsigned)(tb * tmem_half);
+                const unsigned abase = t5_smem_u32(asl + b * 3 * kTsABytes);
+                const unsigned wbase = t5_smem_u32(wsl);
+                unsigned accumulate = kc != 0;
+                const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+                for (int pr = 0; pr < 6; ++pr) {
+#pragma unroll
+                    for (int kk = 0; kk < kTsKT / 16; ++kk) {
+                        if (kc * kTsKT + kk * 16 >= K) continue;  // K-padding half
+                        const uint64_t ad = t5_desc(abase + pa[pr] * kTsABytes + kk * 256, 512);
+                        const uint64_t bd = t5_desc(
+                            wbase + pb[pr] * w_bytes + (kc * 4 + kk * 2) * 128, (Kp / 8) * 128);
+                        t5_mma(d, ad, bd, idesc, accumulate);
+                        accumulate = 1;
+                    }
+                }
+                t5_commit(&sfree[b]);
+                if (kc == KS - 1) t5_commit(&afull[tb]);
+                last = j;
+            }
+            if (*abort_flag && last >= 0)  // committed MMAs finish before TMEM goes (bounded)
+                t5_mbar_wait(&sfree[last & 1], (unsigned)((last >> 1) & 1));
+        }
+    } else {
+        // ------------------------------------------------------- S loader
+        if (lane == 0) {
+            int64_t issued = 0;
+            for (int64_t tj = 0; tj < my_tiles; ++tj) {
+                if (tj >= 1 &&
+                    !t5_mbar_wait_or_abort(stfree, (unsigned)((tj - 1) & 1), abort_flag)) {
+                    fail();
+                    break;
+                }
+                tma_expect_tx(stfull, KS * kQwBox);
+#pragma unroll
+                for (int c3 = 0; c3 < KS; ++c3)
+                    tma_load_2d(stg + c3 * kQwBox, &tmS, 32 * c3, tile_row0(tj), stfull);
+                issued = tj + 1;
+            }
+            if (*abort_flag && issued > 0)  // the last load lands (bounded)
+                t5_mbar_wait(stfull, (unsigned)((issued - 1) & 1));
         }
     }
     t5_fence_before();
@@ -604,14 +925,57 @@ static int launch_tsm_q(cudaStream_t st, int64_t n, float *Qout, int64_t ldo, co
     return check_launch();
 }
 
+template <int NN>
+static int launch_tsm_qw(cudaStream_t st, int64_t n, float *Qout, int64_t ldo, const float *Qin,
+                         int64_t ldq, const float *S, int64_t lds, const double *beta,
+                         int *status) {
+    constexpr int K = 16 * NN;
+    constexpr QwLayout L = qw_layout(K);
+    if ((size_t)L.total > (size_t)max_smem_optin() || n > (int64_t)INT32_MAX - kTsM)
+        return CACG_ERR_UNSUPPORTED;
+    CUtensorMap mq, ms, mo;
+    if (!tma_encode_2d(&mq, Qin, K, (uint64_t)n, (uint64_t)ldq * 4, kTsKT, kTsM,
+                       CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B) ||
+        !tma_encode_2d(&ms, S, K, (uint64_t)n, (uint64_t)lds * 4, kTsKT, kTsM,
+                       CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B) ||
+        !tma_encode_2d(&mo, Qout, K, (uint64_t)n, (uint64_t)ldo * 4, kTsKT, 32,
+                       CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE))
+        return CACG_ERR_UNSUPPORTED;
+    static const bool attr = [] {
+        cudaFuncSetAttribute(tsm_q_tc5w_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)qw_layout(16 * NN).total);
+        return true;
+    }();
+    (void)attr;
+    int tmem_half = 32;
+    while (tmem_half < K) tmem_half *= 2;
+    const int64_t ntiles = (n + kTsM - 1) / kTsM;
+    const int grid = (int)std::min<int64_t>(ntiles, sm_count());
+    tsm_q_tc5w_kernel<NN><<<grid, kQwThreads, L.total, st>>>(mq, ms, mo, n, beta, tmem_half,
+                                                              status);
+    return check_launch();
+}
+
 int launch_qupdate_tc5(cudaStream_t st, int64_t n, int k, float *Qout, int64_t ldo,
                        const float *Qin, int64_t ldq, const float *S, int64_t lds,
-                       const double *beta, int *status) {
+                       const double *beta, int *status, bool allow_tma) {
     if (n < 0 || !beta || !status) return CACG_ERR_ARG;
     if (!tsm_q_tc5_supported(k) || ldq % 4 || ldo % 4 || lds % 4 || !aligned16(Qin) ||
         !aligned16(Qout) || !aligned16(S))
         return CACG_ERR_UNSUPPORTED;
     if (n == 0) return CACG_OK;
+    if (allow_tma) {
+        int rc = CACG_ERR_UNSUPPORTED;
+        switch (k / 16) {
+            case 1: rc = launch_tsm_qw<1>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status); break;
+            case 2: rc = launch_tsm_qw<2>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status); break;
+            case 3: rc = launch_tsm_qw<3>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status); break;
+            case 4: rc = launch_tsm_qw<4>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status); break;
+            case 5: rc = launch_tsm_qw<5>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status); break;
+            case 6: rc = launch_tsm_qw<6>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status); break;
+        }
+        if (rc != CACG_ERR_UNSUPPORTED) return rc;
+    }
     switch (k / 16) {
         case 1: return launch_tsm_q<1>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status);
         case 2: return launch_tsm_q<2>(st, n, Qout, ldo, Qin, ldq, S, lds, beta, status);

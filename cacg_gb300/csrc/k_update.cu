@@ -979,10 +979,12 @@ extern "C" int cacg_k_qupdate(int32_t vtype, int64_t n, int32_t k, void *Q, int6
     } else if (vtype == CACG_VAL_F32) {
         rc = launch_qupdate<float>(st, n, k, (float *)Q, ldq, (const float *)Qin, ldq,
                                    (const float *)S, lds, beta);
-    } else if (vtype == (CACG_VAL_F32 | CACG_VAL_TC5)) {
+    } else if (vtype == (CACG_VAL_F32 | CACG_VAL_TC5) ||
+               vtype == (CACG_VAL_F32 | CACG_VAL_TC5 | CACG_VAL_TC5_CPASYNC)) {
+        const bool tma = (vtype & CACG_VAL_TC5_CPASYNC) == 0;
         rc = run_with_status(st, [&](int *dstat) {
             return launch_qupdate_tc5(st, n, k, (float *)Q, ldq, (const float *)Qin, ldq,
-                                      (const float *)S, lds, beta, dstat);
+                                      (const float *)S, lds, beta, dstat, tma);
         });
     } else {
         rc = CACG_ERR_ARG;

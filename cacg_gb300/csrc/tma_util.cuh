@@ -66,6 +66,28 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
         "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(tma_smem_u32(bar))
         : "memory");
 }
+
+// 2-D tiled TMA store of the box at (x, y) from src (rows outside the tensor
+// are not written); completion is tracked by the calling thread's bulk groups
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, int x, int y,
+                                             const void *src) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];\n" ::"l"(
+            reinterpret_cast<uint64_t>(map)),
+        "r"(x), "r"(y), "r"(tma_smem_u32(src))
+        : "memory");
+}
+__device__ __forceinline__ void tma_store_commit() {
+    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+}
+// the shared-memory sources of this thread's committed stores have been read
+__device__ __forceinline__ void tma_store_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+}
+// this thread's committed stores are complete
+__device__ __forceinline__ void tma_store_wait_all() {
+    asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+}
 #endif
 
 }  // namespace cacg

@@ -86,6 +86,8 @@ extern "C" {
                             FP32 accumulation).  Returns CACG_ERR_UNSUPPORTED outside
                             qupdate: k % 16 == 0, k <= 96; xrupdate: k % 4 == 0,
                             k <= 256, m <= 16 dividing 32; both: 16-byte aligned rows */
+#define CACG_VAL_TC5_CPASYNC 64 /* with CACG_VAL_TC5 in cacg_k_qupdate: the cp.async-fed
+                                   kernel instead of the TMA-fed one (bit-identical) */
 
 /* generators (cacg_gen_*) */
 #define CACG_GEN_LAPLACE2D_5PT 1
