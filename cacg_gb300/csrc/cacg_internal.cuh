@@ -81,6 +81,21 @@ __device__ __forceinline__ void vstore(float *p, const float (&d)[4]) {
     *reinterpret_cast<float4 *>(p) = make_float4(d[0], d[1], d[2], d[3]);
 }
 
+// a0 += v x0, a1 += v x1 as one packed FP32 FMA (fma.rn.f32x2, sm_100 and
+// later): two independent round-to-nearest FMAs, bit-identical to fmaf
+__device__ __forceinline__ void fma2_bcast(float &a0, float &a1, float v, float x0, float x1) {
+    asm("{\n"
+        ".reg .b64 va, xa, ac;\n"
+        "mov.b64 va, {%2, %2};\n"
+        "mov.b64 xa, {%3, %4};\n"
+        "mov.b64 ac, {%0, %1};\n"
+        "fma.rn.f32x2 ac, va, xa, ac;\n"
+        "mov.b64 {%0, %1}, ac;\n"
+        "}\n"
+        : "+f"(a0), "+f"(a1)
+        : "f"(v), "f"(x0), "f"(x1));
+}
+
 inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
 // ------------------------------------------------------ bf16 slice planes
@@ -232,6 +247,11 @@ int launch_xrupdate_sl(cudaStream_t st, int64_t n, int k, int m, const float *Q,
 int launch_xrupdate_m16(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
                         int64_t ldq, const double *alpha, double *X, double *R, float *S0,
                         int64_t lds, float *R32, double *norms, double *ws);
+// the same with Q and AQ fed by TMA (k % 4 == 0, k <= 128, 16-byte aligned
+// operands and row strides); *status gets kStatusTimeout if a bounded wait expires
+int launch_xrupdate_m16_tma(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
+                            int64_t ldq, const double *alpha, double *X, double *R, float *S0,
+                            int64_t lds, float *R32, double *norms, double *ws, int *status);
 
 template <typename T>
 int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,

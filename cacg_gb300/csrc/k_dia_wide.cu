@@ -41,20 +41,6 @@ __device__ __forceinline__ void wide_cp16(void *smem, const void *g, int bytes) 
                  "l"(g), "r"(bytes));
 }
 
-// a0 += v x0, a1 += v x1 as one packed FP32 FMA (two round-to-nearest FMAs)
-__device__ __forceinline__ void wide_fma2(float &a0, float &a1, float v, float x0, float x1) {
-    asm("{\n"
-        ".reg .b64 va, xa, ac;\n"
-        "mov.b64 va, {%2, %2};\n"
-        "mov.b64 xa, {%3, %4};\n"
-        "mov.b64 ac, {%0, %1};\n"
-        "fma.rn.f32x2 ac, va, xa, ac;\n"
-        "mov.b64 {%0, %1}, ac;\n"
-        "}\n"
-        : "+f"(a0), "+f"(a1)
-        : "f"(v), "f"(x0), "f"(x1));
-}
-
 // Y = ca A X + cb Z1 + cc Z2, all n x COLS row-major (row stride COLS)
 template <int COLS>
 __global__ void __launch_bounds__(kWideThreads, kWideCtas)
@@ -141,8 +127,8 @@ __global__ void __launch_bounds__(kWideThreads, kWideCtas)
 #pragma unroll
                     for (int i = 0; i < kWideR; ++i) {
                         const float4 x = win[i + j];
-                        wide_fma2(acc[i][0], acc[i][1], vv[i], x.x, x.y);
-                        wide_fma2(acc[i][2], acc[i][3], vv[i], x.z, x.w);
+                        fma2_bcast(acc[i][0], acc[i][1], vv[i], x.x, x.y);
+                        fma2_bcast(acc[i][2], acc[i][3], vv[i], x.z, x.w);
                     }
                 }
             }

@@ -1012,12 +1012,22 @@ extern "C" int cacg_k_xrupdate(int32_t vtype, int64_t n, int32_t k, int32_t m, c
                    : launch_xrupdate_fast<double>(st, n, k, m, (const double *)Q,
                                                   (const double *)AQ, ldq, alpha, X, R,
                                                   (double *)S0, lds, nullptr, norms, ws);
-    else if (vtype == CACG_VAL_F32)
-        rc = exact ? launch_xrupdate<float>(st, n, k, m, (const float *)Q, (const float *)AQ, ldq,
-                                            alpha, X, R, (float *)S0, lds, nullptr, norms, ws)
-                   : launch_xrupdate_fast<float>(st, n, k, m, (const float *)Q,
-                                                 (const float *)AQ, ldq, alpha, X, R,
-                                                 (float *)S0, lds, nullptr, norms, ws);
+    else if (vtype == CACG_VAL_F32 && exact)
+        rc = launch_xrupdate<float>(st, n, k, m, (const float *)Q, (const float *)AQ, ldq, alpha,
+                                    X, R, (float *)S0, lds, nullptr, norms, ws);
+    else if (vtype == CACG_VAL_F32) {
+        rc = CACG_ERR_UNSUPPORTED;
+        if (m == 16)  // TMA-fed kernel where the operands allow it
+            rc = run_with_status(st, [&](int *dstat) {
+                return launch_xrupdate_m16_tma(st, n, k, (const float *)Q, (const float *)AQ, ldq,
+                                               alpha, X, R, (float *)S0, lds, nullptr, norms, ws,
+                                               dstat);
+            });
+        if (rc == CACG_ERR_UNSUPPORTED)
+            rc = launch_xrupdate_fast<float>(st, n, k, m, (const float *)Q, (const float *)AQ,
+                                             ldq, alpha, X, R, (float *)S0, lds, nullptr, norms,
+                                             ws);
+    }
     else if (vtype == (CACG_VAL_F32 | CACG_VAL_TC5) && !exact)
         rc = run_with_status(st, [&](int *dstat) {
             return launch_xrupdate_tc5(st, n, k, m, (const float *)Q, (const float *)AQ, ldq, alpha,

@@ -24,6 +24,8 @@
 
 #include "cacg_internal.cuh"
 #include "ff_util.cuh"
+#include "tc5_util.cuh"
+#include "tma_util.cuh"
 
 namespace cacg {
 
@@ -149,9 +151,262 @@ __global__ void __launch_bounds__(kXr16Threads)
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same update with Q and AQ fed by TMA (16-byte aligned operands and row
+// strides).  Persistent CTAs walk 128-row tiles: a loader thread streams each
+// tile's Q and AQ as 32-column boxes (128-byte swizzle) into a ring of two
+// or more stages; eight compute warps take 16 rows each, a thread two rows x
+// output columns 4c .. 4c + 3 over all k (no cross-lane reduction).  Per
+// chunk of four coefficients a thread reads one 16-byte piece of each of its
+// Q and AQ rows (swizzled positions: the eight rows a warp reads at once hit
+// distinct banks) and four alpha rows (FP32, broadcast); the FMAs go out as
+// packed pairs (fma.rn.f32x2), summing over k in increasing order.
+// X and R (128-byte FP64 rows) are read with coalesced loads issued before
+// the stage wait, and the epilogue is that of xrupdate16_kernel.
+constexpr int kXtWarps = 8;                       // compute warps
+constexpr int kXtSlots = 8 * kXtWarps;            // row slots (a thread's first row)
+constexpr int kXtThreads = 32 * (kXtWarps + 1);   // + the loader warp
+constexpr int kXtMaxStages = 4;
+// two rows a thread (rows rl and rl + 64 of a 128-row tile): twice the
+// independent FMA chains and half the alpha loads per FMA of one row a
+// thread (0.61 ms against 0.79 ms per outer iteration at 128^3, k = 96)
+constexpr int kXtRpt = 2;
+
+__host__ __device__ constexpr size_t xt_smem(int nbx, int rpt, int stages) {
+    return (size_t)stages * 2 * nbx * (kXtSlots * rpt * 128) + (size_t)32 * nbx * 16 * 4 +
+           (size_t)kXtSlots * 16 * 8 + 16 * kXtMaxStages + 16;
+}
+
+template <int NBX>  // 32-column boxes per operand: k <= 32 NBX
+__global__ void __launch_bounds__(kXtThreads, 1)
+    xrupdate16_tma_kernel(const __grid_constant__ CUtensorMap tmQ,
+                          const __grid_constant__ CUtensorMap tmAQ, int64_t n, int k, int stages,
+                          const double *__restrict__ alpha, double *__restrict__ X,
+                          double *__restrict__ R, float *__restrict__ S0, int64_t lds,
+                          float *__restrict__ R32, double *__restrict__ part,
+                          int *__restrict__ status) {
+    constexpr int KP = 32 * NBX;
+    constexpr int RPT = kXtRpt;
+    constexpr int kXtRows = kXtSlots * RPT;            // rows per tile
+    constexpr unsigned kXtBox = kXtRows * 32 * 4;       // one box: tile rows x 32 columns
+    constexpr unsigned stage_bytes = 2 * NBX * kXtBox;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // [ring: stages x (Q boxes, AQ boxes)][alpha KP x 16 FP32][norm partials
+    // 64 x 16 FP64][full, empty mbarriers][abort]
+    unsigned char *ring = smem_raw;
+    float *al = reinterpret_cast<float *>(ring + (size_t)stages * stage_bytes);
+    double *red = reinterpret_cast<double *>(al + KP * 16);
+    uint64_t *full = reinterpret_cast<uint64_t *>(red + kXtSlots * 16);
+    uint64_t *empty = full + kXtMaxStages;
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(empty + kXtMaxStages);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < KP * 16; i += kXtThreads) {
+        const int j = i >> 4;
+        al[i] = j < k ? (float)alpha[i] : 0.f;  // alpha is k x 16, row-major
+    }
+    if (tid == 0) {
+        for (int q = 0; q < stages; ++q) {
+            t5_mbar_init(&full[q], 1);
+            t5_mbar_init(&empty[q], kXtWarps);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    const int64_t ntiles = (n + kXtRows - 1) / kXtRows;
+    const int64_t my_tiles =
+        ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    auto fail = [&]() {
+        *abort_flag = 1;
+        atomicOr(status, kStatusTimeout);
+    };
+
+    if (warp == kXtWarps) {
+        // ---------------------------------------------------------- loader
+        if (lane == 0) {
+            int64_t issued = 0;
+            for (int64_t t = 0; t < my_tiles; ++t) {
+                const int q = (int)(t % stages);
+                if (t >= stages &&
+                    !t5_mbar_wait_or_abort(&empty[q], (unsigned)(((t / stages) - 1) & 1),
+                                           abort_flag)) {
+                    fail();
+                    break;
+                }
+                unsigned char *dst = ring + (size_t)q * stage_bytes;
+                const int y = (int)((blockIdx.x + t * gridDim.x) * kXtRows);
+                tma_expect_tx(&full[q], stage_bytes);
+#pragma unroll
+                for (int b = 0; b < NBX; ++b) {
+                    tma_load_2d(dst + b * kXtBox, &tmQ, 32 * b, y, &full[q]);
+                    tma_load_2d(dst + (NBX + b) * kXtBox, &tmAQ, 32 * b, y, &full[q]);
+                }
+                issued = t + 1;
+            }
+            if (*abort_flag)  // the loads in flight land before the CTA exits (bounded)
+                for (int64_t t = issued > stages ? issued - stages : 0; t < issued; ++t)
+                    t5_mbar_wait(&full[t % stages], (unsigned)((t / stages) & 1));
+        }
+    } else {
+        // ---------------------------------------------------------- compute
+        // thread rows rl + kXtSlots i (same swizzle phase), columns 4c .. 4c + 3
+        const int rl = 8 * warp + (lane >> 2), c4 = lane & 3;
+        const int sw = rl & 7;
+        float sq_hi[4] = {0.f, 0.f, 0.f, 0.f}, sq_lo[4] = {0.f, 0.f, 0.f, 0.f};
+        bool ok = true;
+        for (int64_t t = 0; t < my_tiles; ++t) {
+            const int q = (int)(t % stages);
+            const int64_t row0 = (blockIdx.x + t * gridDim.x) * (int64_t)kXtRows + rl;
+            double2 xo[RPT][2], ro[RPT][2];
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                const int64_t row = row0 + kXtSlots * i;
+                xo[i][0] = xo[i][1] = ro[i][0] = ro[i][1] = make_double2(0.0, 0.0);
+                if (row < n) {
+                    const double *xp = X + row * 16 + 4 * c4, *rp = R + row * 16 + 4 * c4;
+                    xo[i][0] = *reinterpret_cast<const double2 *>(xp);
+                    xo[i][1] = *reinterpret_cast<const double2 *>(xp + 2);
+                    ro[i][0] = *reinterpret_cast<const double2 *>(rp);
+                    ro[i][1] = *reinterpret_cast<const double2 *>(rp + 2);
+                }
+            }
+            const bool w =
+                t5_mbar_wait_or_abort(&full[q], (unsigned)((t / stages) & 1), abort_flag);
+            if (!__all_sync(0xffffffffu, w)) {
+                ok = false;
+                break;
+            }
+            const unsigned char *stq = ring + (size_t)q * stage_bytes + rl * 128;
+            float ax[RPT][4], ar[RPT][4];
+#pragma unroll
+            for (int i = 0; i < RPT; ++i)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) ax[i][c] = ar[i][c] = 0.f;
+#pragma unroll
+            for (int b = 0; b < NBX; ++b) {
+                const unsigned char *qrow = stq + b * kXtBox;
+                const unsigned char *arow = stq + (NBX + b) * kXtBox;
+#pragma unroll
+                for (int ch = 0; ch < 8; ++ch) {
+                    float4 qv[RPT], av[RPT];
+#pragma unroll
+                    for (int i = 0; i < RPT; ++i) {
+                        const int off = kXtSlots * 128 * i + ((ch ^ sw) << 4);
+                        qv[i] = *reinterpret_cast<const float4 *>(qrow + off);
+                        av[i] = *reinterpret_cast<const float4 *>(arow + off);
+                    }
+                    const float *ap = al + (32 * b + 4 * ch) * 16 + 4 * c4;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const float4 wv = *reinterpret_cast<const float4 *>(ap + 16 * u);
+#pragma unroll
+                        for (int i = 0; i < RPT; ++i) {
+                            const float qs = u == 0 ? qv[i].x : u == 1 ? qv[i].y : u == 2 ? qv[i].z : qv[i].w;
+                            const float as = u == 0 ? av[i].x : u == 1 ? av[i].y : u == 2 ? av[i].z : av[i].w;
+                            fma2_bcast(ax[i][0], ax[i][1], qs, wv.x, wv.y);
+                            fma2_bcast(ax[i][2], ax[i][3], qs, wv.z, wv.w);
+                            fma2_bcast(ar[i][0], ar[i][1], as, wv.x, wv.y);
+                            fma2_bcast(ar[i][2], ar[i][3], as, wv.z, wv.w);
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane == 0) t5_mbar_arrive(&empty[q]);  // this warp's rows of the stage are read
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                const int64_t row = row0 + kXtSlots * i;
+                if (row >= n) break;
+                const double xv[4] = {xo[i][0].x, xo[i][0].y, xo[i][1].x, xo[i][1].y};
+                const double rv[4] = {ro[i][0].x, ro[i][0].y, ro[i][1].x, ro[i][1].y};
+                double xn[4], rn[4];
+                float rf[4];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    xn[c] = xv[c] + ff_widen(ax[i][c]);
+                    rn[c] = rv[c] - ff_widen(ar[i][c]);
+                    rf[c] = ff_narrow(rn[c]);
+                    float rh, rlo;
+                    ff_split_bits(rn[c], rh, rlo);
+                    ff_add_square(rh, rlo, sq_hi[c], sq_lo[c]);
+                }
+                double *xp = X + row * 16 + 4 * c4, *rp = R + row * 16 + 4 * c4;
+                *reinterpret_cast<double2 *>(xp) = make_double2(xn[0], xn[1]);
+                *reinterpret_cast<double2 *>(xp + 2) = make_double2(xn[2], xn[3]);
+                *reinterpret_cast<double2 *>(rp) = make_double2(rn[0], rn[1]);
+                *reinterpret_cast<double2 *>(rp + 2) = make_double2(rn[2], rn[3]);
+                const float4 r4 = make_float4(rf[0], rf[1], rf[2], rf[3]);
+                if (S0) *reinterpret_cast<float4 *>(S0 + row * lds + 4 * c4) = r4;
+                if (R32) *reinterpret_cast<float4 *>(R32 + row * 16 + 4 * c4) = r4;
+            }
+        }
+        if (!ok && lane == 0) fail();
+#pragma unroll
+        for (int c = 0; c < 4; ++c) red[rl * 16 + 4 * c4 + c] = ff_widen(sq_hi[c]) + ff_widen(sq_lo[c]);
+    }
+    __syncthreads();
+    if (part && tid < 16) {
+        double s = 0.0;
+        for (int r = 0; r < kXtSlots; ++r) s += red[r * 16 + tid];
+        part[(size_t)blockIdx.x * 16 + tid] = s;
+    }
+}
+
+template <int NBX>
+int launch_xt(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ, int64_t ldq,
+              const double *alpha, double *X, double *R, float *S0, int64_t lds, float *R32,
+              double *norms, double *ws, int *status) {
+    constexpr int kXtRows = kXtSlots * kXtRpt;
+    const size_t budget = (size_t)max_smem_optin();
+    int stages = kXtMaxStages;
+    while (stages > 2 && xt_smem(NBX, kXtRpt, stages) > budget) --stages;
+    const size_t smem = xt_smem(NBX, kXtRpt, stages);
+    if (smem > budget || n > (int64_t)INT32_MAX - kXtRows) return CACG_ERR_UNSUPPORTED;
+    CUtensorMap mq, ma;
+    if (!tma_encode_2d(&mq, Q, (uint64_t)k, (uint64_t)n, (uint64_t)ldq * 4, 32, kXtRows,
+                       CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B) ||
+        !tma_encode_2d(&ma, AQ, (uint64_t)k, (uint64_t)n, (uint64_t)ldq * 4, 32, kXtRows,
+                       CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B))
+        return CACG_ERR_UNSUPPORTED;
+    static const bool attr = [] {
+        cudaFuncSetAttribute(xrupdate16_tma_kernel<NBX>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem_optin());
+        return true;
+    }();
+    (void)attr;
+    const int64_t ntiles = (n + kXtRows - 1) / kXtRows;
+    const int grid =
+        (int)std::min<int64_t>(ntiles, std::min<int64_t>(sm_count(), kXr16MaxBlocks));
+    xrupdate16_tma_kernel<NBX><<<grid, kXtThreads, smem, st>>>(
+        mq, ma, n, k, stages, alpha, X, R, S0, lds, R32, norms ? ws : nullptr, status);
+    int rc = check_launch();
+    if (rc != CACG_OK || !norms) return rc;
+    return launch_colsum(st, ws, grid, 16, norms);
+}
+
 bool a16(const void *p) { return ((uintptr_t)p & 15) == 0; }
 
 }  // namespace
+
+int launch_xrupdate_m16_tma(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
+                            int64_t ldq, const double *alpha, double *X, double *R, float *S0,
+                            int64_t lds, float *R32, double *norms, double *ws, int *status) {
+    if (k <= 0 || k % 4 != 0 || k > 128 || ldq % 4 || !a16(Q) || !a16(AQ) || !a16(X) ||
+        !a16(R) || !status)
+        return CACG_ERR_UNSUPPORTED;
+    if (S0 && (lds % 4 || lds < 16 || !a16(S0))) return CACG_ERR_UNSUPPORTED;
+    if (R32 && !a16(R32)) return CACG_ERR_UNSUPPORTED;
+    if (norms && !ws) return CACG_ERR_ARG;
+    if (n <= 0) return CACG_ERR_UNSUPPORTED;
+    switch ((k + 31) / 32) {
+        case 1: return launch_xt<1>(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms, ws, status);
+        case 2: return launch_xt<2>(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms, ws, status);
+        case 3: return launch_xt<3>(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms, ws, status);
+        case 4: return launch_xt<4>(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms, ws, status);
+    }
+    return CACG_ERR_UNSUPPORTED;
+}
 
 int launch_xrupdate_m16(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
                         int64_t ldq, const double *alpha, double *X, double *R, float *S0,

@@ -821,7 +821,15 @@ struct Solver {
             return launch_xrupdate<T>(st, A->n, k, m, Q, AQ, k, b.alpha, X, b.R, (T *)b.S, k,
                                       b.R32, b.norms, b.norm_ws);
         // (the tcgen05 X/R update, launch_xrupdate_tc5, is slower than the
-        // CUDA-core kernel at m = 16: its N = 16 MMAs are latency-bound)
+        // CUDA-core kernels at m = 16: its N = 16 MMAs are latency-bound)
+        if constexpr (std::is_same<T, float>::value) {
+            if (m == 16) {
+                int rc = launch_xrupdate_m16_tma(st, A->n, k, Q, AQ, k, b.alpha, X, b.R,
+                                                 (float *)b.S, k, b.R32, b.norms, b.norm_ws,
+                                                 b.status);
+                if (rc != CACG_ERR_UNSUPPORTED) return rc;
+            }
+        }
         return launch_xrupdate_fast<T>(st, A->n, k, m, Q, AQ, k, b.alpha, X, b.R, (T *)b.S, k,
                                        b.R32, b.norms, b.norm_ws);
     }

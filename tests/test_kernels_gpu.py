@@ -275,6 +275,35 @@ def test_xrupdate(lib, torch_cuda, vt, exact, n, k, m):
     assert relerr(host(norms), (Rg * Rg).sum(axis=0)) <= 1e-13
 
 
+@pytest.mark.parametrize("n,k", [(130001, 96), (999, 48), (5000, 100), (3001, 128), (64, 16),
+                                 (20000, 96)])
+def test_xrupdate_m16_tma(lib, torch_cuda, n, k):
+    """FP32, 16 right-hand sides: the TMA-fed X/R update (64-row tiles, rows
+    not a multiple of the tile, k not a multiple of the 32-column box) within
+    the FP32-product tolerance; S0 = (float)R; norms of the new R in FP64."""
+    torch = torch_cuda
+    m = 16
+    Q = O.gen_rhs("normal", n, k, 21).astype(np.float32)
+    AQ = O.gen_rhs("normal", n, k, 22).astype(np.float32)
+    al = O.gen_rhs("normal", k, m, 23)
+    X = O.gen_rhs("normal", n, m, 24)
+    R = O.gen_rhs("normal", n, m, 25)
+    Xw = X + O.port_tallsmall(Q.astype(np.float64), al)
+    Rw = R - O.port_tallsmall(AQ.astype(np.float64), al)
+    dQ, dAQ, dal, dX, dR = (dev(torch, a) for a in (Q, AQ, al, X, R))
+    S0 = torch.zeros((n, k), dtype=torch.float32, device="cuda")
+    norms = torch.zeros(m, dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_xrupdate(F32, n, k, m, ptr(dQ), ptr(dAQ), k, ptr(dal), ptr(dX), ptr(dR),
+                             ptr(S0), k, ptr(norms), None)
+    assert rc == 0
+    assert relerr(host(dX), Xw) <= 5e-6
+    assert relerr(host(dR), Rw) <= 5e-6
+    Rg = host(dR)
+    assert relerr(host(S0)[:, :m], Rg) <= 1e-7
+    assert np.all(host(S0)[:, m:] == 0)
+    assert relerr(host(norms), (Rg * Rg).sum(axis=0)) <= 1e-13
+
+
 @pytest.mark.parametrize("n,k,m", [(10000, 64, 8), (20000, 96, 16), (777, 4, 1),
                                    (3000, 20, 4), (4000, 256, 16), (130001, 96, 16),
                                    (5001, 32, 2)])
