@@ -582,6 +582,192 @@ __global__ void __launch_bounds__(kDiaThreads, 2)
     }
 }
 
+// The same float-float residual for m = 16 with the row stride fixed at
+// compile time (window rows at immediate offsets, no clamping inside the
+// matrix) and the float-float products and sums on packed FP32 pairs
+// (two columns per instruction: mul/fma/add/sub .rn.f32x2).  Every pair lane
+// computes exactly what ff_mac computes for its column -- the product is
+// formed as -p = (-a) x so that e = fma(a, x, -p) needs no negation -- so the
+// result is bit-identical to dia_resid_ff_kernel.
+__device__ __forceinline__ unsigned long long ff_pack(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void ff_unpack(unsigned long long v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+// (sh, sl) += a x over two columns: a = ah + al (broadcast A, NA = -A, AL),
+// x = xh + xl (pairs)
+__device__ __forceinline__ void ff_mac2(unsigned long long &sh, unsigned long long &sl,
+                                        unsigned long long A, unsigned long long NA,
+                                        unsigned long long AL, unsigned long long xh,
+                                        unsigned long long xl) {
+    asm("{\n"
+        ".reg .b64 np, e, t, s, bp, t1, t2, t3, er, u;\n"
+        "mul.rn.f32x2 np, %3, %5;\n"      // -p
+        "fma.rn.f32x2 e, %2, %5, np;\n"   // e = a xh - p (exact)
+        "fma.rn.f32x2 t, %4, %5, e;\n"    // al xh + e
+        "fma.rn.f32x2 t, %2, %6, t;\n"    // ah xl + (al xh + e)
+        "sub.rn.f32x2 s, %0, np;\n"       // s = sh + p
+        "sub.rn.f32x2 bp, s, %0;\n"       // bp = s - sh
+        "sub.rn.f32x2 t1, s, bp;\n"
+        "sub.rn.f32x2 t2, %0, t1;\n"      // sh - (s - bp)
+        "add.rn.f32x2 t3, np, bp;\n"      // -(p - bp)
+        "sub.rn.f32x2 er, t2, t3;\n"      // (sh - (s - bp)) + (p - bp)
+        "add.rn.f32x2 u, er, t;\n"
+        "add.rn.f32x2 %1, %1, u;\n"
+        "mov.b64 %0, s;\n"
+        "}\n"
+        : "+l"(sh), "+l"(sl)
+        : "l"(A), "l"(NA), "l"(AL), "l"(xh), "l"(xl));
+}
+
+constexpr int kRf16R = 4;          // rows per thread
+constexpr int kRf16Runs = 64;      // runs per block (256 threads, 4 per row)
+
+__global__ void __launch_bounds__(kDiaThreads, 2)
+    dia_resid_ff16_kernel(int64_t n, int64_t npad, const __grid_constant__ DiaDesc desc,
+                          const float *__restrict__ vals, const float *__restrict__ Xh,
+                          const float *__restrict__ Xl, const double *__restrict__ B,
+                          double *__restrict__ Rout, float *__restrict__ S0, int64_t lds,
+                          float *__restrict__ R32, double *__restrict__ part) {
+    constexpr int M = 16, R = kRf16R, BR = kRf16Runs * R;
+    constexpr int W = R + kDiaGroupMax - 1;
+    extern __shared__ __align__(16) unsigned char dia_smem[];
+    float *vs = reinterpret_cast<float *>(dia_smem);  // [2][2 nd][BR]: hi rows, then lo rows
+    __shared__ int64_t g_off[kDiaMax];                 // group offset x M
+    __shared__ int g_d0[kDiaMax], g_size[kDiaMax];
+    const int nd = desc.ndiag, nd2 = 2 * nd, ng = desc.ngroups;
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+        g_off[g] = desc.off[desc.gstart[g]] * M;
+        g_d0[g] = desc.gstart[g];
+        g_size[g] = desc.gstart[g + 1] - desc.gstart[g];
+    }
+    const int lr = threadIdx.x >> 2, c = threadIdx.x & 3;
+    const int64_t nblk = (n + BR - 1) / BR;
+    const int64_t omin = desc.off[0], omax = desc.off[nd - 1];
+
+    auto stage = [&](int64_t blk, int buf) {
+        if (blk < nblk) {
+            float *dst = vs + (size_t)buf * nd2 * BR;
+            constexpr int per = BR / 4;
+            for (int idx = threadIdx.x; idx < nd2 * per; idx += kDiaThreads) {
+                const int d = idx / per, q = idx - d * per;
+                const int64_t e0 = blk * BR + (int64_t)q * 4;
+                const int64_t left = npad - e0;
+                const int by = left >= 4 ? 16 : (left > 0 ? (int)left * 4 : 0);
+                dia_cp16(dst + (size_t)d * BR + q * 4,
+                         by ? (const void *)(vals + (size_t)d * npad + e0) : vals, by);
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::);
+    };
+
+    double sq[4] = {0.0, 0.0, 0.0, 0.0};
+    int buf = 0;
+    stage(blockIdx.x, 0);
+    for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x, buf ^= 1) {
+        stage(blk + gridDim.x, buf ^ 1);
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncthreads();
+        const int64_t r0 = blk * BR + (int64_t)lr * R;
+        const bool inside = blk * BR + omin >= 0 && blk * BR + BR - 1 + omax < n;
+        unsigned long long sh[R][2], sl[R][2];
+#pragma unroll
+        for (int i = 0; i < R; ++i) sh[i][0] = sh[i][1] = sl[i][0] = sl[i][1] = 0ull;
+        for (int g = 0; g < ng; ++g) {
+            const int G = g_size[g];
+            ulonglong2 wh[W], wl[W];
+            if (inside) {
+                const int64_t e = r0 * M + g_off[g] + 4 * c;
+                const ulonglong2 *ph = reinterpret_cast<const ulonglong2 *>(Xh + e);
+                const ulonglong2 *pl = reinterpret_cast<const ulonglong2 *>(Xl + e);
+#pragma unroll
+                for (int t = 0; t < W; ++t)
+                    if (t < R + G - 1) {
+                        wh[t] = __ldg(ph + t * (M / 4));
+                        wl[t] = __ldg(pl + t * (M / 4));
+                    }
+            } else {
+                const int64_t x0 = r0 + g_off[g] / M;
+#pragma unroll
+                for (int t = 0; t < W; ++t)
+                    if (t < R + G - 1) {
+                        int64_t xr = x0 + t;
+                        xr = xr < 0 ? 0 : (xr >= n ? n - 1 : xr);  // value is 0 there
+                        wh[t] = __ldg(reinterpret_cast<const ulonglong2 *>(Xh + xr * M + 4 * c));
+                        wl[t] = __ldg(reinterpret_cast<const ulonglong2 *>(Xl + xr * M + 4 * c));
+                    }
+            }
+            const float *vg = vs + ((size_t)buf * nd2 + g_d0[g]) * BR + lr * R;
+#pragma unroll
+            for (int j = 0; j < kDiaGroupMax; ++j) {
+                if (j < G) {
+                    const float4 vh = *reinterpret_cast<const float4 *>(vg + j * BR);
+                    const float4 vl = *reinterpret_cast<const float4 *>(vg + (size_t)nd * BR + j * BR);
+                    const float ah[R] = {vh.x, vh.y, vh.z, vh.w}, al[R] = {vl.x, vl.y, vl.z, vl.w};
+#pragma unroll
+                    for (int i = 0; i < R; ++i) {
+                        const unsigned long long A = ff_pack(ah[i], ah[i]);
+                        const unsigned long long NA = ff_pack(-ah[i], -ah[i]);
+                        const unsigned long long AL = ff_pack(al[i], al[i]);
+                        ff_mac2(sh[i][0], sl[i][0], A, NA, AL, wh[i + j].x, wl[i + j].x);
+                        ff_mac2(sh[i][1], sl[i][1], A, NA, AL, wh[i + j].y, wl[i + j].y);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+            const int64_t row = r0 + i;
+            if (row >= n) break;
+            const int64_t col = 4 * c;
+            const double2 b01 = *reinterpret_cast<const double2 *>(B + row * M + col);
+            const double2 b23 = *reinterpret_cast<const double2 *>(B + row * M + col + 2);
+            const double bv[4] = {b01.x, b01.y, b23.x, b23.y};
+            float shv[4], slv[4];
+            ff_unpack(sh[i][0], shv[0], shv[1]);
+            ff_unpack(sh[i][1], shv[2], shv[3]);
+            ff_unpack(sl[i][0], slv[0], slv[1]);
+            ff_unpack(sl[i][1], slv[2], slv[3]);
+            double rd[4];
+            float rf[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float bh, bl;
+                ff_split_bits(bv[q], bh, bl);
+                const float s = bh - shv[q];
+                const float bp = s - bh;
+                const float err = (bh - (s - bp)) + (-shv[q] - bp);
+                const float lo = err + (bl - slv[q]);
+                rd[q] = ff_widen(s) + ff_widen(lo);
+                rf[q] = s + lo;
+                const double w = ff_widen(rf[q]);
+                sq[q] = fma(w, w, sq[q]);
+            }
+            *reinterpret_cast<double2 *>(Rout + row * M + col) = make_double2(rd[0], rd[1]);
+            *reinterpret_cast<double2 *>(Rout + row * M + col + 2) = make_double2(rd[2], rd[3]);
+            if (S0) vstore(S0 + row * lds + col, rf);
+            if (R32) vstore(R32 + row * M + col, rf);
+        }
+        __syncthreads();  // buffer `buf` is refilled two blocks on
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    if (part) {
+        __syncthreads();
+        double *red = reinterpret_cast<double *>(dia_smem);  // runs x 16
+#pragma unroll
+        for (int q = 0; q < 4; ++q) red[(size_t)lr * M + c * 4 + q] = sq[q];
+        __syncthreads();
+        if (threadIdx.x < M) {
+            double t = 0.0;
+            for (int r = 0; r < kRf16Runs; ++r) t += red[(size_t)r * M + threadIdx.x];
+            part[(size_t)blockIdx.x * M + threadIdx.x] = t;
+        }
+    }
+}
+
 // Float-float residual (see above); CACG_ERR_UNSUPPORTED when the matrix has
 // no FP32 hi/lo view or m is not a multiple of 4.  Xh, Xl: n x m scratch.
 int launch_dia_residual_ff(cudaStream_t st, const DevMatrix *A, int m, const double *X,
@@ -610,9 +796,20 @@ int launch_dia_residual_ff(cudaStream_t st, const DevMatrix *A, int m, const dou
     static const bool attr = [] {
         cudaFuncSetAttribute(dia_resid_ff_kernel<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              200 * 1024);
+        cudaFuncSetAttribute(dia_resid_ff16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
         return true;
     }();
     (void)attr;
+    if (m == 16 && A->dia.ngroups <= kDiaMax &&
+        runs_per_block == kRf16Runs && BR == kRf16Runs * kRf16R) {
+        dia_resid_ff16_kernel<<<(unsigned)blocks, kDiaThreads, smem, st>>>(
+            A->n, A->dia_npad, A->dia, A->dia32, Xh, Xl, B, R, S0, lds, R32,
+            norms ? ws : nullptr);
+        rc = check_launch();
+        if (rc != CACG_OK || !norms) return rc;
+        return launch_colsum(st, ws, (int)blocks, m, norms);
+    }
     dia_resid_ff_kernel<RR><<<(unsigned)blocks, kDiaThreads, smem, st>>>(
         A->n, A->dia_npad, A->dia, A->dia32, cpr, runs_per_block, Xh, Xl, m, B, R, S0, lds, R32,
         norms ? ws : nullptr);
