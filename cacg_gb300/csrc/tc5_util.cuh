@@ -175,18 +175,32 @@ __device__ __forceinline__ int t5_bar_or(int id, int count, int pred) {
 
 // x0, x1 -> three bf16x2 words (high, middle, low slices; round-to-nearest
 // at each split, so x = h + m + l up to the last slice's rounding).
+// The two residual subtractions run as packed FP32 pairs (sub.rn.f32x2); the
+// widening of a bf16 pair is exact bit placement, so the words equal those of
+// the scalar sequence.
 __device__ __forceinline__ void t5_split2(float x0, float x1, unsigned &hw, unsigned &mw,
                                           unsigned &lw) {
-    const float2 v = make_float2(x0, x1);
-    const __nv_bfloat162 h = __float22bfloat162_rn(v);
-    const float2 hf = __bfloat1622float2(h);
-    const float2 r1 = make_float2(v.x - hf.x, v.y - hf.y);
-    const __nv_bfloat162 m = __float22bfloat162_rn(r1);
-    const float2 mf = __bfloat1622float2(m);
-    const __nv_bfloat162 l = __float22bfloat162_rn(make_float2(r1.x - mf.x, r1.y - mf.y));
-    hw = t5_bits(h);
-    mw = t5_bits(m);
-    lw = t5_bits(l);
+    asm("{\n"
+        ".reg .b32 wl, wh;\n"
+        ".reg .b64 v, w, r;\n"
+        ".reg .f32 ra, rb;\n"
+        "cvt.rn.bf16x2.f32 %0, %4, %3;\n"   // x1 -> high half, x0 -> low half
+        "shl.b32 wl, %0, 16;\n"
+        "and.b32 wh, %0, 0xFFFF0000;\n"
+        "mov.b64 v, {%3, %4};\n"
+        "mov.b64 w, {wl, wh};\n"
+        "sub.rn.f32x2 r, v, w;\n"
+        "mov.b64 {ra, rb}, r;\n"
+        "cvt.rn.bf16x2.f32 %1, rb, ra;\n"
+        "shl.b32 wl, %1, 16;\n"
+        "and.b32 wh, %1, 0xFFFF0000;\n"
+        "mov.b64 w, {wl, wh};\n"
+        "sub.rn.f32x2 r, r, w;\n"
+        "mov.b64 {ra, rb}, r;\n"
+        "cvt.rn.bf16x2.f32 %2, rb, ra;\n"
+        "}\n"
+        : "=r"(hw), "=r"(mw), "=r"(lw)
+        : "f"(x0), "f"(x1));
 }
 
 }  // namespace cacg
