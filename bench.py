@@ -419,8 +419,8 @@ def run_serving(args):
 # (n = 884,736; per-kernel table with the command in
 # profiles/ncu_traffic_st27_96_m16.md); every figure is linear in n at fixed
 # m and s.
-TRAFFIC_96 = {"basis_spmm": 297.2e6, "aq_spmm": 737.2e6, "qupdate": 963.0e6,
-              "xrupdate": 1210.2e6 + 0.1e6, "gram": (679.8e6 + 736.7e6) / 2 + 12.2e6}
+TRAFFIC_96 = {"basis_spmm": 297.8e6, "aq_spmm": 732.9e6, "qupdate": 963.5e6,
+              "xrupdate": 1210.7e6, "gram": (679.7e6 + 739.7e6) / 2 + 12.2e6}
 TRAFFIC_96_N = 884736
 
 

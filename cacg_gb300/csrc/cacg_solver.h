@@ -68,9 +68,10 @@ int launch_dia_ring(cudaStream_t st, const DevMatrix *A, int w, const float *X, 
                     float *Y, int64_t ldy, const float *Z1, int64_t ldz1, const float *Z2,
                     int64_t ldz2, double ca, double cb, double cc, int *status);
 
-// The same product for FP32 blocks whose width (64 or 96) is also their row
-// stride, with compile-time strides (k_dia_wide.cu); bit-identical to
-// launch_dia_spmm.  CACG_ERR_UNSUPPORTED for other shapes.
+// The same product without recurrence terms (Z1 = Z2 = NULL: the A Q product)
+// for FP32 blocks whose width (64 or 96) is also their row stride, with
+// compile-time strides (k_dia_wide.cu); bit-identical to launch_dia_spmm.
+// CACG_ERR_UNSUPPORTED for other shapes.
 int launch_dia_wide(cudaStream_t st, const DevMatrix *A, int w, const float *X, int64_t ldx,
                     float *Y, int64_t ldy, const float *Z1, int64_t ldz1, const float *Z2,
                     int64_t ldz2, double ca, double cb, double cc);

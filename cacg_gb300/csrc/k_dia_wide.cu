@@ -41,13 +41,12 @@ __device__ __forceinline__ void wide_cp16(void *smem, const void *g, int bytes) 
                  "l"(g), "r"(bytes));
 }
 
-// Y = ca A X + cb Z1 + cc Z2, all n x COLS row-major (row stride COLS)
+// Y = ca A X, both n x COLS row-major (row stride COLS)
 template <int COLS>
 __global__ void __launch_bounds__(kWideThreads, kWideCtas)
     dia_wide_kernel(int64_t n, int64_t npad, const __grid_constant__ DiaDesc desc,
                     const float *__restrict__ vals, const float *__restrict__ X,
-                    float *__restrict__ Y, const float *__restrict__ Z1,
-                    const float *__restrict__ Z2, float ca, float cb, float cc) {
+                    float *__restrict__ Y, float ca) {
     constexpr int CPR = COLS / 4;                 // 16-byte chunks per row
     constexpr int RUNS = kWideThreads / CPR;      // row runs per block
     constexpr int BR = RUNS * kWideR;             // rows per block
@@ -141,20 +140,6 @@ __global__ void __launch_bounds__(kWideThreads, kWideCtas)
 #pragma unroll
             for (int q = 0; q < 4; ++q) y[q] = ca * acc[i][q];
             const int64_t e = row * COLS + 4 * c;
-            if (Z1) {
-                const float4 z = *reinterpret_cast<const float4 *>(Z1 + e);
-                y[0] = fmaf(cb, z.x, y[0]);
-                y[1] = fmaf(cb, z.y, y[1]);
-                y[2] = fmaf(cb, z.z, y[2]);
-                y[3] = fmaf(cb, z.w, y[3]);
-            }
-            if (Z2) {
-                const float4 z = *reinterpret_cast<const float4 *>(Z2 + e);
-                y[0] = fmaf(cc, z.x, y[0]);
-                y[1] = fmaf(cc, z.y, y[1]);
-                y[2] = fmaf(cc, z.z, y[2]);
-                y[3] = fmaf(cc, z.w, y[3]);
-            }
             *reinterpret_cast<float4 *>(Y + e) = make_float4(y[0], y[1], y[2], y[3]);
         }
         __syncthreads();  // buffer `buf` is refilled two blocks on
@@ -163,8 +148,7 @@ __global__ void __launch_bounds__(kWideThreads, kWideCtas)
 }
 
 template <int COLS>
-int launch_wide(cudaStream_t st, const DevMatrix *A, const float *X, float *Y, const float *Z1,
-                const float *Z2, float ca, float cb, float cc) {
+int launch_wide(cudaStream_t st, const DevMatrix *A, const float *X, float *Y, float ca) {
     constexpr int BR = (kWideThreads / (COLS / 4)) * kWideR;
     const size_t smem = 2 * (size_t)A->dia_ndiag * BR * sizeof(float);
     if (smem > 96 * 1024) return CACG_ERR_UNSUPPORTED;
@@ -177,7 +161,7 @@ int launch_wide(cudaStream_t st, const DevMatrix *A, const float *X, float *Y, c
     const int64_t nblk = (A->n + BR - 1) / BR;
     const int64_t blocks = std::min<int64_t>(nblk, (int64_t)sm_count() * kWideCtas);
     dia_wide_kernel<COLS><<<(unsigned)blocks, kWideThreads, smem, st>>>(
-        A->n, A->dia_npad, A->dia, A->dia32, X, Y, Z1, Z2, ca, cb, cc);
+        A->n, A->dia_npad, A->dia, A->dia32, X, Y, ca);
     return check_launch();
 }
 
@@ -190,16 +174,17 @@ int launch_dia_wide(cudaStream_t st, const DevMatrix *A, int w, const float *X, 
                     int64_t ldz2, double ca, double cb, double cc) {
     if (!A || A->dia_ndiag <= 0 || !A->dia32 || A->dia.ngroups > kDiaMax)
         return CACG_ERR_UNSUPPORTED;
-    if (ldx != w || ldy != w || (Z1 && ldz1 != w) || (Z2 && ldz2 != w))
-        return CACG_ERR_UNSUPPORTED;
-    if (!a16w(X) || !a16w(Y) || (Z1 && !a16w(Z1)) || (Z2 && !a16w(Z2)))
-        return CACG_ERR_UNSUPPORTED;
+    // the A Q product only: no recurrence terms (the basis steps take the rings)
+    if (Z1 || Z2 || cb != 0.0 || cc != 0.0) return CACG_ERR_UNSUPPORTED;
+    (void)ldz1;
+    (void)ldz2;
+    if (ldx != w || ldy != w || !a16w(X) || !a16w(Y)) return CACG_ERR_UNSUPPORTED;
     if (A->n <= 0) return CACG_OK;
     switch (w) {
         case 96:
-            return launch_wide<96>(st, A, X, Y, Z1, Z2, (float)ca, (float)cb, (float)cc);
+            return launch_wide<96>(st, A, X, Y, (float)ca);
         case 64:
-            return launch_wide<64>(st, A, X, Y, Z1, Z2, (float)ca, (float)cb, (float)cc);
+            return launch_wide<64>(st, A, X, Y, (float)ca);
         default:
             return CACG_ERR_UNSUPPORTED;
     }
