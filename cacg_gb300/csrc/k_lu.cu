@@ -17,9 +17,13 @@
 // A zero or non-finite pivot sets *status = 1 (CACG_ERR_BREAKDOWN at the
 // host) instead of trapping; the arithmetic continues as the reference's
 // does (inf/NaN propagate) and the host stops the iteration.
+#include <cooperative_groups.h>
+
 #include "cacg_internal.cuh"
 
 namespace cacg {
+
+namespace cgrp = cooperative_groups;
 
 constexpr int kLuThreads = 512;
 constexpr int kLuSmemK = 144;  // factor in shared memory up to k = 144 (162 KB)
@@ -67,6 +71,74 @@ __global__ void __launch_bounds__(kLuThreads)
         FT[idx] = W[(size_t)j * k + i];
     }
     if (threadIdx.x == 0 && bad && status) atomicOr(status, kStatusBreakdown);
+}
+
+// The same factor spread over a cluster of kLucCtas CTAs (one SM each): CTA r
+// owns rows i = r (mod kLucCtas) in its shared memory.  Step d: the owner of
+// row d scales it by the pivot's reciprocal; one cluster barrier; every CTA
+// copies the scaled row d from the owner's shared memory (distributed shared
+// memory) and updates its rows i > d.  Every element sees the same
+// operations in the same order as lu_factor_kernel (bit-identical factors);
+// the trailing update's FP64 work is split over kLucCtas SMs' FP64 pipes.
+constexpr int kLucCtas = 8;
+constexpr int kLucThreads = 256;
+constexpr int kLucMaxK = 256;
+
+__global__ void __cluster_dims__(kLucCtas, 1, 1) __launch_bounds__(kLucThreads)
+    lu_factor_cluster_kernel(int k, const double *__restrict__ M, double *__restrict__ F,
+                             int *__restrict__ status) {
+    extern __shared__ __align__(16) double luc_sm[];
+    cgrp::cluster_group cluster = cgrp::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int nloc = (k - rank + kLucCtas - 1) / kLucCtas;  // rows rank, rank + C, ...
+    const int rows_max = (k + kLucCtas - 1) / kLucCtas;
+    double *Wl = luc_sm;                        // nloc x k: local rows
+    double *prow = luc_sm + (size_t)rows_max * k;  // the current pivot row
+    for (int idx = threadIdx.x; idx < nloc * k; idx += blockDim.x) {
+        const int li = idx / k, c = idx - li * k;
+        Wl[idx] = M[(size_t)(li * kLucCtas + rank) * k + c];
+    }
+    double *Dinv = F + (size_t)k * k;
+    int bad = 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    for (int d = 0; d < k; ++d) {
+        const int owner = d % kLucCtas;
+        if (rank == owner && warp == 0) {
+            double *rd = Wl + (size_t)(d / kLucCtas) * k;
+            double inv = 0.0;
+            if (lane == 0) {
+                const double piv = rd[d];
+                if (piv == 0.0 || !isfinite(piv)) bad = 1;
+                inv = 1.0 / piv;
+                Dinv[d] = inv;
+            }
+            inv = __shfl_sync(0xffffffffu, inv, 0);
+            for (int c = d + 1 + lane; c < k; c += 32) rd[c] *= inv;
+        }
+        cluster.sync();  // row d scaled, visible to the cluster
+        const double *src = cluster.map_shared_rank(Wl + (size_t)(d / kLucCtas) * k, owner);
+        for (int c = d + 1 + threadIdx.x; c < k; c += blockDim.x) prow[c] = src[c];
+        __syncthreads();
+        // local rows i > d: rows by warp, columns by lane
+        const int li0 = (d + 1 - rank + kLucCtas - 1) / kLucCtas;  // first local row past d
+        for (int li = li0 + warp; li < nloc; li += kLucThreads / 32) {
+            double *wi = Wl + (size_t)li * k;
+            const double lid = wi[d];
+            for (int c = d + 1 + lane; c < k; c += 32) wi[c] = wi[c] - lid * prow[c];
+        }
+        __syncthreads();
+    }
+    // factors and their transpose (the column-sweep solves read FT)
+    double *FT = F + (size_t)k * k + k;
+    for (int idx = threadIdx.x; idx < nloc * k; idx += blockDim.x) {
+        const int li = idx / k, c = idx - li * k;
+        const int i = li * kLucCtas + rank;
+        F[(size_t)i * k + c] = Wl[idx];
+        FT[(size_t)c * k + i] = Wl[idx];
+    }
+    if (threadIdx.x == 0 && bad && status) atomicOr(status, kStatusBreakdown);
+    cluster.sync();  // no CTA leaves while another may still read its rows
 }
 
 // Y (k x r) from the factor F (k*k factors + k reciprocal diagonal) and RHS
@@ -215,6 +287,20 @@ static int launch_sweep(cudaStream_t st, int k, const double *F, int r, const do
 
 int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *status) {
     if (k <= 0) return CACG_ERR_ARG;
+    if (k >= kLucCtas && k <= kLucMaxK) {
+        const size_t csmem = ((size_t)((k + kLucCtas - 1) / kLucCtas) * k + k) * sizeof(double);
+        static const bool cattr = [] {
+            cudaFuncSetAttribute(lu_factor_cluster_kernel,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(((size_t)(kLucMaxK / kLucCtas) * kLucMaxK + kLucMaxK) *
+                                       sizeof(double)));
+            return true;
+        }();
+        (void)cattr;
+        lu_factor_cluster_kernel<<<kLucCtas, kLucThreads, csmem, st>>>(k, M, F, status);
+        if (cudaGetLastError() == cudaSuccess) return CACG_OK;
+        // cluster launch refused: the one-CTA factor below
+    }
     int use_smem = k <= kLuSmemK;
     size_t smem = use_smem ? (size_t)k * k * sizeof(double) : 0;
     static const bool attr = [] {

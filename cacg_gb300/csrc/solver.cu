@@ -632,6 +632,9 @@ struct Solver {
     // R = B - A X (FP64); S0 = cast(R); R32; norms.  Used at start and for
     // residual replacement / true-residual checks.
     bool slices = false;
+    // the X whose FP64 residual b.R holds (nullptr once X may have changed):
+    // the final true residual then needs only its norms
+    const double *r_fp64_of = nullptr;
 
     // R = B - A X.  ff: in the mixed mode over a DIA view, float-float
     // arithmetic (FP32 pipe) instead of FP64 -- used for the periodic residual
@@ -667,6 +670,7 @@ struct Solver {
                                           prec == CACG_MIXED, k, norms, b.norm_ws);
             if (rc == CACG_OK && write_s0 && b.R32)
                 rc = launch_cast_f64_f32(st, A->n * m, R, b.R32);
+            if (rc == CACG_OK && R == b.R) r_fp64_of = X;
         }
         prof.end();
         return rc;
@@ -850,6 +854,7 @@ struct Solver {
     int run(const double *B, double *X, cacg_result *res) {
         const int64_t n = A->n;
         int rc;
+        r_fp64_of = nullptr;
         res->status = CACG_OK;
         res->iterations = 0;
         res->residual_replacements = 0;
@@ -898,6 +903,7 @@ struct Solver {
         GraphPair gp;
         const bool prof_on = prof.on;
         for (it = 0; it < p.maxit; ++it) {
+            r_fp64_of = nullptr;  // this iteration updates X
             if (graphs && it >= 2) {
                 const int par = it & 1;
                 prof.on = false;
@@ -969,8 +975,10 @@ struct Solver {
                 }
             }
         }
-        // final true residual per column (FP64)
-        rc = spmm<double>(X, m, b.R, m, m, B, m, nullptr, 0, -1.0, 1.0, 0.0);
+        // final true residual per column (FP64); after a converged FP64 check
+        // b.R already holds B - A X for this X
+        rc = r_fp64_of == X ? CACG_OK
+                            : spmm<double>(X, m, b.R, m, m, B, m, nullptr, 0, -1.0, 1.0, 0.0);
         if (rc == CACG_OK)
             rc = launch_residual_post(st, n, m, b.R, nullptr, 0, k, b.tnorm, b.norm_ws);
         if (rc) return rc;
