@@ -298,8 +298,8 @@ int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *st
         }();
         (void)cattr;
         lu_factor_cluster_kernel<<<kLucCtas, kLucThreads, csmem, st>>>(k, M, F, status);
-        if (cudaGetLastError() == cudaSuccess) return CACG_OK;
-        // cluster launch refused: the one-CTA factor below
+        if (cudaPeekAtLastError() == cudaSuccess) return check_launch();  // counted
+        cudaGetLastError();  // cluster launch refused: the one-CTA factor below
     }
     int use_smem = k <= kLuSmemK;
     size_t smem = use_smem ? (size_t)k * k * sizeof(double) : 0;
