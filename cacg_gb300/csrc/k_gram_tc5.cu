@@ -513,9 +513,12 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
             return true;
         };
         bool ok = true;
+        // ring stage and its phase, stepped (no division by the runtime depth)
+        int q = 0;
+        unsigned qph = 0;
         for (int64_t j = 0; j < nsteps && ok; ++j) {
-            const int q = (int)(j % stages), b = (int)(j % kT5wNB);
-            bool w = t5_mbar_wait_or_abort(&full[q], (unsigned)((j / stages) & 1), abort_flag);
+            const int b = (int)(j % kT5wNB);
+            bool w = t5_mbar_wait_or_abort(&full[q], qph, abort_flag);
             if (w && j >= kT5wNB)
                 w = t5_mbar_wait_or_abort(&sfree[b], (unsigned)(((j / kT5wNB) - 1) & 1), abort_flag);
             if (!__all_sync(0xffffffffu, w)) {
@@ -553,6 +556,10 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
                 t5_mbar_arrive(&sfull[b]);
                 t5_mbar_arrive(&empty[q]);
             }
+            if (++q == stages) {
+                q = 0;
+                qph ^= 1u;
+            }
             if (j >= 2 && group_end(j - 2)) ok = flush_group(j - 2);
         }
         // the last groups' sums
@@ -562,10 +569,11 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
     } else if (tid == kT5wConv) {
         // ---------------------------------------------------------- loader
         int64_t issued = 0;
+        int q = 0;
+        unsigned qph = 0;  // phase of stage q's current fill
         for (int64_t j = 0; j < nsteps; ++j) {
-            const int q = (int)(j % stages);
-            if (j >= stages &&
-                !t5_mbar_wait_or_abort(&empty[q], (unsigned)(((j / stages) - 1) & 1), abort_flag)) {
+            if (j > 0 && q == 0) qph ^= 1u;
+            if (j >= stages && !t5_mbar_wait_or_abort(&empty[q], qph ^ 1u, abort_flag)) {
                 fail();
                 break;
             }
@@ -581,6 +589,7 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
                 tma_load_2d(dst + (nbl + nbr1 + bx) * kT5mBoxBytes, &tmR2, c2 + kT5mBox * bx, row0,
                             &full[q]);
             issued = j + 1;
+            if (++q == stages) q = 0;
         }
         if (*abort_flag)  // let the loads in flight land (bounded)
             for (int64_t j = issued - stages > 0 ? issued - stages : 0; j < issued; ++j)

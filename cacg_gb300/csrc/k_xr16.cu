@@ -226,11 +226,11 @@ __global__ void __launch_bounds__(kXtThreads, 1)
         // ---------------------------------------------------------- loader
         if (lane == 0) {
             int64_t issued = 0;
+            int q = 0;
+            unsigned qph = 0;  // phase of stage q's current fill (stepped, no division)
             for (int64_t t = 0; t < my_tiles; ++t) {
-                const int q = (int)(t % stages);
-                if (t >= stages &&
-                    !t5_mbar_wait_or_abort(&empty[q], (unsigned)(((t / stages) - 1) & 1),
-                                           abort_flag)) {
+                if (t > 0 && q == 0) qph ^= 1u;
+                if (t >= stages && !t5_mbar_wait_or_abort(&empty[q], qph ^ 1u, abort_flag)) {
                     fail();
                     break;
                 }
@@ -243,6 +243,7 @@ __global__ void __launch_bounds__(kXtThreads, 1)
                     tma_load_2d(dst + (NBX + b) * kXtBox, &tmAQ, 32 * b, y, &full[q]);
                 }
                 issued = t + 1;
+                if (++q == stages) q = 0;
             }
             if (*abort_flag)  // the loads in flight land before the CTA exits (bounded)
                 for (int64_t t = issued > stages ? issued - stages : 0; t < issued; ++t)
@@ -255,8 +256,9 @@ __global__ void __launch_bounds__(kXtThreads, 1)
         const int sw = rl & 7;
         float sq_hi[4] = {0.f, 0.f, 0.f, 0.f}, sq_lo[4] = {0.f, 0.f, 0.f, 0.f};
         bool ok = true;
+        int q = 0;
+        unsigned qph = 0;
         for (int64_t t = 0; t < my_tiles; ++t) {
-            const int q = (int)(t % stages);
             const int64_t row0 = (blockIdx.x + t * gridDim.x) * (int64_t)kXtRows + rl;
             double2 xo[RPT][2], ro[RPT][2];
 #pragma unroll
@@ -271,8 +273,7 @@ __global__ void __launch_bounds__(kXtThreads, 1)
                     ro[i][1] = *reinterpret_cast<const double2 *>(rp + 2);
                 }
             }
-            const bool w =
-                t5_mbar_wait_or_abort(&full[q], (unsigned)((t / stages) & 1), abort_flag);
+            const bool w = t5_mbar_wait_or_abort(&full[q], qph, abort_flag);
             if (!__all_sync(0xffffffffu, w)) {
                 ok = false;
                 break;
@@ -314,6 +315,10 @@ __global__ void __launch_bounds__(kXtThreads, 1)
             }
             __syncwarp();
             if (lane == 0) t5_mbar_arrive(&empty[q]);  // this warp's rows of the stage are read
+            if (++q == stages) {
+                q = 0;
+                qph ^= 1u;
+            }
 #pragma unroll
             for (int i = 0; i < RPT; ++i) {
                 const int64_t row = row0 + kXtSlots * i;
