@@ -252,6 +252,11 @@ int launch_xrupdate_m16(cudaStream_t st, int64_t n, int k, const float *Q, const
 int launch_xrupdate_m16_tma(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
                             int64_t ldq, const double *alpha, double *X, double *R, float *S0,
                             int64_t lds, float *R32, double *norms, double *ws, int *status);
+// the same on the float-float state: X and R as FP32 pairs (n x 16 high
+// parts, then n x 16 low parts); no FP64 instruction
+int launch_xrupdate_m16_ff(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
+                           int64_t ldq, const double *alpha, float *Xff, float *Rff, float *S0,
+                           int64_t lds, float *R32, double *norms, double *ws, int *status);
 
 template <typename T>
 int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, const T *AQ,

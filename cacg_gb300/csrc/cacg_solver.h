@@ -46,12 +46,17 @@ struct DevMatrix {
 
 int launch_dia_hilo(cudaStream_t st, int64_t count, const double *v64, float *hi, float *lo);
 int launch_ff_split(cudaStream_t st, int64_t count, const double *x, float *hi, float *lo);
+// x = hi + lo in FP64 (k_dia.cu)
+int launch_ff_join(cudaStream_t st, int64_t count, const float *hi, const float *lo, double *x);
 // R = B - A X in float-float over the DIA view, with S0 = R32 = (float)R and
-// the column norms of R; Xh, Xl: n x m FP32 scratch (k_dia.cu)
+// the column norms of R; Xh, Xl: n x m FP32 scratch, filled from X (X ==
+// NULL: they already hold X).  Rff != NULL (m = 16): R written as a
+// normalised float-float pair (n x 16 high parts, then low parts) instead of
+// FP64 R (k_dia.cu)
 int launch_dia_residual_ff(cudaStream_t st, const DevMatrix *A, int m, const double *X,
                            const double *B, double *R, float *Xh, float *Xl, float *S0,
                            int64_t lds, float *R32, double *norms, double *ws,
-                           int64_t ws_doubles);
+                           int64_t ws_doubles, float *Rff = nullptr);
 
 // Y = ca A X + cb Z1 + cc Z2 over the DIA view (k_dia.cu);
 // CACG_ERR_UNSUPPORTED when the matrix has no view of this precision.

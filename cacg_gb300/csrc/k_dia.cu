@@ -224,6 +224,22 @@ int launch_ff_split(cudaStream_t st, int64_t count, const double *x, float *hi, 
     return check_launch();
 }
 
+// x = hi + lo in FP64 (the float-float state back to FP64: exact widenings,
+// one rounding)
+__global__ void ff_join_kernel(int64_t count, const float *__restrict__ hi,
+                               const float *__restrict__ lo, double *__restrict__ x) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = ff_widen(hi[i]) + ff_widen(lo[i]);
+}
+
+int launch_ff_join(cudaStream_t st, int64_t count, const float *hi, const float *lo, double *x) {
+    if (count <= 0) return CACG_OK;
+    const int blocks = (int)std::min<int64_t>((count + 255) / 256, (int64_t)sm_count() * 16);
+    ff_join_kernel<<<blocks, 256, 0, st>>>(count, hi, lo, x);
+    return check_launch();
+}
+
 // FP32 hi/lo view from the FP64 view (matrices created without FP32 values)
 __global__ void dia_hilo_kernel(int64_t count, const double *__restrict__ v64,
                                 float *__restrict__ hi, float *__restrict__ lo) {
@@ -630,8 +646,11 @@ __global__ void __launch_bounds__(kDiaThreads, 2)
     dia_resid_ff16_kernel(int64_t n, int64_t npad, const __grid_constant__ DiaDesc desc,
                           const float *__restrict__ vals, const float *__restrict__ Xh,
                           const float *__restrict__ Xl, const double *__restrict__ B,
-                          double *__restrict__ Rout, float *__restrict__ S0, int64_t lds,
-                          float *__restrict__ R32, double *__restrict__ part) {
+                          double *__restrict__ Rout, float *__restrict__ Rff,
+                          float *__restrict__ S0, int64_t lds, float *__restrict__ R32,
+                          double *__restrict__ part) {
+    // Rff (n x 16 high parts, then n x 16 low parts): R as a normalised
+    // float-float pair instead of FP64 Rout, norms in float-float
     constexpr int M = 16, R = kRf16R, BR = kRf16Runs * R;
     constexpr int W = R + kDiaGroupMax - 1;
     extern __shared__ __align__(16) unsigned char dia_smem[];
@@ -665,6 +684,7 @@ __global__ void __launch_bounds__(kDiaThreads, 2)
     };
 
     double sq[4] = {0.0, 0.0, 0.0, 0.0};
+    float fq_hi[4] = {0.f, 0.f, 0.f, 0.f}, fq_lo[4] = {0.f, 0.f, 0.f, 0.f};
     int buf = 0;
     stage(blockIdx.x, 0);
     for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x, buf ^= 1) {
@@ -732,7 +752,7 @@ __global__ void __launch_bounds__(kDiaThreads, 2)
             ff_unpack(sl[i][0], slv[0], slv[1]);
             ff_unpack(sl[i][1], slv[2], slv[3]);
             double rd[4];
-            float rf[4];
+            float rf[4], rl[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 float bh, bl;
@@ -741,13 +761,25 @@ __global__ void __launch_bounds__(kDiaThreads, 2)
                 const float bp = s - bh;
                 const float err = (bh - (s - bp)) + (-shv[q] - bp);
                 const float lo = err + (bl - slv[q]);
-                rd[q] = ff_widen(s) + ff_widen(lo);
                 rf[q] = s + lo;
-                const double w = ff_widen(rf[q]);
-                sq[q] = fma(w, w, sq[q]);
+                if (Rff) {  // normalised pair (TwoSum: s may have cancelled)
+                    const float tp = rf[q] - s;
+                    rl[q] = (s - (rf[q] - tp)) + (lo - tp);
+                    ff_add_square(rf[q], rl[q], fq_hi[q], fq_lo[q]);
+                } else {
+                    rd[q] = ff_widen(s) + ff_widen(lo);
+                    const double w = ff_widen(rf[q]);
+                    sq[q] = fma(w, w, sq[q]);
+                }
             }
-            *reinterpret_cast<double2 *>(Rout + row * M + col) = make_double2(rd[0], rd[1]);
-            *reinterpret_cast<double2 *>(Rout + row * M + col + 2) = make_double2(rd[2], rd[3]);
+            if (Rff) {
+                vstore(Rff + row * M + col, rf);
+                vstore(Rff + (n + row) * M + col, rl);
+            } else {
+                *reinterpret_cast<double2 *>(Rout + row * M + col) = make_double2(rd[0], rd[1]);
+                *reinterpret_cast<double2 *>(Rout + row * M + col + 2) =
+                    make_double2(rd[2], rd[3]);
+            }
             if (S0) vstore(S0 + row * lds + col, rf);
             if (R32) vstore(R32 + row * M + col, rf);
         }
@@ -758,7 +790,9 @@ __global__ void __launch_bounds__(kDiaThreads, 2)
         __syncthreads();
         double *red = reinterpret_cast<double *>(dia_smem);  // runs x 16
 #pragma unroll
-        for (int q = 0; q < 4; ++q) red[(size_t)lr * M + c * 4 + q] = sq[q];
+        for (int q = 0; q < 4; ++q)
+            red[(size_t)lr * M + c * 4 + q] =
+                Rff ? ff_widen(fq_hi[q]) + ff_widen(fq_lo[q]) : sq[q];
         __syncthreads();
         if (threadIdx.x < M) {
             double t = 0.0;
@@ -773,10 +807,11 @@ __global__ void __launch_bounds__(kDiaThreads, 2)
 int launch_dia_residual_ff(cudaStream_t st, const DevMatrix *A, int m, const double *X,
                            const double *B, double *R, float *Xh, float *Xl, float *S0,
                            int64_t lds, float *R32, double *norms, double *ws,
-                           int64_t ws_doubles) {
+                           int64_t ws_doubles, float *Rff) {
     if (!A || A->dia_ndiag <= 0 || !A->dia32 || !A->dia32lo || m % 4 != 0 || m <= 0)
         return CACG_ERR_UNSUPPORTED;
-    if (!aligned16(X) || !aligned16(B) || !aligned16(R) || !aligned16(Xh) || !aligned16(Xl) ||
+    if ((X && !aligned16(X)) || !aligned16(B) || (!R && !Rff) || (R && !aligned16(R)) ||
+        (Rff && (m != 16 || !aligned16(Rff))) || !aligned16(Xh) || !aligned16(Xl) ||
         (S0 && (lds % 4 || !aligned16(S0))) || (R32 && !aligned16(R32)))
         return CACG_ERR_UNSUPPORTED;
     constexpr int RR = kDiaR / 2;
@@ -791,7 +826,11 @@ int launch_dia_residual_ff(cudaStream_t st, const DevMatrix *A, int m, const dou
     const int per_sm = std::max(1, std::min(2, (int)(220 * 1024 / smem)));
     const int64_t blocks = std::min<int64_t>(nblk, (int64_t)sm_count() * per_sm);
     if (norms && (int64_t)blocks * m > ws_doubles) return CACG_ERR_UNSUPPORTED;
-    int rc = launch_ff_split(st, A->n * (int64_t)m, X, Xh, Xl);
+    const bool k16 = m == 16 && A->dia.ngroups <= kDiaMax && runs_per_block == kRf16Runs &&
+                     BR == kRf16Runs * kRf16R;
+    if (Rff && !k16) return CACG_ERR_UNSUPPORTED;
+    // X == NULL: Xh, Xl already hold X
+    int rc = X ? launch_ff_split(st, A->n * (int64_t)m, X, Xh, Xl) : CACG_OK;
     if (rc != CACG_OK) return rc;
     static const bool attr = [] {
         cudaFuncSetAttribute(dia_resid_ff_kernel<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -801,10 +840,9 @@ int launch_dia_residual_ff(cudaStream_t st, const DevMatrix *A, int m, const dou
         return true;
     }();
     (void)attr;
-    if (m == 16 && A->dia.ngroups <= kDiaMax &&
-        runs_per_block == kRf16Runs && BR == kRf16Runs * kRf16R) {
+    if (k16) {
         dia_resid_ff16_kernel<<<(unsigned)blocks, kDiaThreads, smem, st>>>(
-            A->n, A->dia_npad, A->dia, A->dia32, Xh, Xl, B, R, S0, lds, R32,
+            A->n, A->dia_npad, A->dia, A->dia32, Xh, Xl, B, Rff ? nullptr : R, Rff, S0, lds, R32,
             norms ? ws : nullptr);
         rc = check_launch();
         if (rc != CACG_OK || !norms) return rc;

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kRingThreads + 32, 2)
                     const float *__restrict__ Z2, int64_t ldz2, float ca, float cb, float cc,
                     int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char ring_smem[];
-    // full[2]: block u's loads landed (TMA); done[2]: the four compute warps
+    // full[2]: block u's loads landed (TMA); done[2]: all 128 compute threads
     // finished block u (its ring slots and value buffer may be refilled)
     uint64_t *full = reinterpret_cast<uint64_t *>(ring_smem + rd.boff);
     uint64_t *done = full + 2;
@@ -152,8 +152,8 @@ __global__ void __launch_bounds__(kRingThreads + 32, 2)
     if (tid == 0) {
         t5_mbar_init(&full[0], 1);
         t5_mbar_init(&full[1], 1);
-        t5_mbar_init(&done[0], kRingThreads / 32);
-        t5_mbar_init(&done[1], kRingThreads / 32);
+        t5_mbar_init(&done[0], kRingThreads);  // every compute thread releases
+        t5_mbar_init(&done[1], kRingThreads);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         t5_fence_proxy_async();
@@ -315,9 +315,11 @@ __global__ void __launch_bounds__(kRingThreads + 32, 2)
                     if (base[b] >= rd.cap[b]) base[b] -= rd.cap[b];
                 }
             }
-            // this warp is done with the block's ring slots and values
-            __syncwarp();
-            if ((tid & 31) == 0) t5_mbar_arrive(&done[u & 1]);
+            // this thread is done with the block's ring slots and values: each
+            // thread orders its own shared-memory reads before the producer's
+            // next TMA fill of these slots (proxy fence, then its arrive)
+            t5_fence_proxy_async();
+            t5_mbar_arrive(&done[u & 1]);
         }
     }
 }

@@ -1004,7 +1004,19 @@ extern "C" int cacg_k_xrupdate(int32_t vtype, int64_t n, int32_t k, int32_t m, c
     int rc;
     // vtype | CACG_XR_EXACT selects the float-float product sums
     const bool exact = (vtype & CACG_XR_EXACT) != 0;
-    vtype &= ~CACG_XR_EXACT;
+    const bool ffstate = (vtype & CACG_XR_FFSTATE) != 0;
+    vtype &= ~(CACG_XR_EXACT | CACG_XR_FFSTATE);
+    if (ffstate) {  // float-float X and R (TMA-fed kernel only)
+        int rc2 = CACG_ERR_ARG;
+        if (vtype == CACG_VAL_F32 && !exact && m == 16)
+            rc2 = run_with_status(st, [&](int *dstat) {
+                return launch_xrupdate_m16_ff(st, n, k, (const float *)Q, (const float *)AQ, ldq,
+                                              alpha, (float *)X, (float *)R, (float *)S0, lds,
+                                              nullptr, norms, ws, dstat);
+            });
+        cudaFreeAsync(ws, st);
+        return rc2;
+    }
     if (vtype == CACG_VAL_F64)
         rc = exact ? launch_xrupdate<double>(st, n, k, m, (const double *)Q, (const double *)AQ,
                                              ldq, alpha, X, R, (double *)S0, lds, nullptr,

@@ -177,14 +177,35 @@ __host__ __device__ constexpr size_t xt_smem(int nbx, int rpt, int stages) {
            (size_t)kXtSlots * 16 * 8 + 16 * kXtMaxStages + 16;
 }
 
-template <int NBX>  // 32-column boxes per operand: k <= 32 NBX
+// (hi, lo) + b as a float-float pair, renormalised (two TwoSums: exact
+// error of hi + b, then of the sum with the low parts; no ordering assumed,
+// since R cancels heavily near convergence)
+__device__ __forceinline__ void ff_add_float(float &hi, float &lo, float b) {
+    const float s = hi + b;
+    const float bp = s - hi;
+    const float e = (hi - (s - bp)) + (b - bp);
+    const float l = e + lo;
+    const float t = s + l;
+    const float tp = t - s;
+    lo = (s - (t - tp)) + (l - tp);
+    hi = t;
+}
+
+// FF = false: X, R FP64 (n x 16).  FF = true: X and R as float-float pairs,
+// each n x 16 high parts followed by n x 16 low parts (the mixed solve's
+// state between FP64 checks): the updates are float-float additions on the
+// FP32 pipe, no FP64 instruction.
+template <int NBX, bool FF>  // 32-column boxes per operand: k <= 32 NBX
 __global__ void __launch_bounds__(kXtThreads, 1)
     xrupdate16_tma_kernel(const __grid_constant__ CUtensorMap tmQ,
                           const __grid_constant__ CUtensorMap tmAQ, int64_t n, int k, int stages,
-                          const double *__restrict__ alpha, double *__restrict__ X,
-                          double *__restrict__ R, float *__restrict__ S0, int64_t lds,
+                          const double *__restrict__ alpha, void *__restrict__ Xv,
+                          void *__restrict__ Rv, float *__restrict__ S0, int64_t lds,
                           float *__restrict__ R32, double *__restrict__ part,
                           int *__restrict__ status) {
+    double *X = static_cast<double *>(Xv), *R = static_cast<double *>(Rv);
+    float *Xh = static_cast<float *>(Xv), *Rh = static_cast<float *>(Rv);
+    float *Xl = Xh + n * 16, *Rl = Rh + n * 16;
     constexpr int KP = 32 * NBX;
     constexpr int RPT = kXtRpt;
     constexpr int kXtRows = kXtSlots * RPT;            // rows per tile
@@ -208,7 +229,7 @@ __global__ void __launch_bounds__(kXtThreads, 1)
     if (tid == 0) {
         for (int q = 0; q < stages; ++q) {
             t5_mbar_init(&full[q], 1);
-            t5_mbar_init(&empty[q], kXtWarps);
+            t5_mbar_init(&empty[q], kXtWarps * 32);  // every compute thread releases
         }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -260,17 +281,29 @@ __global__ void __launch_bounds__(kXtThreads, 1)
         unsigned qph = 0;
         for (int64_t t = 0; t < my_tiles; ++t) {
             const int64_t row0 = (blockIdx.x + t * gridDim.x) * (int64_t)kXtRows + rl;
-            double2 xo[RPT][2], ro[RPT][2];
+            double2 xo[RPT][2], ro[RPT][2];   // FP64 state
+            float4 xhv[RPT], xlv[RPT], rhv[RPT], rlv[RPT];  // float-float state
 #pragma unroll
             for (int i = 0; i < RPT; ++i) {
                 const int64_t row = row0 + kXtSlots * i;
-                xo[i][0] = xo[i][1] = ro[i][0] = ro[i][1] = make_double2(0.0, 0.0);
-                if (row < n) {
-                    const double *xp = X + row * 16 + 4 * c4, *rp = R + row * 16 + 4 * c4;
-                    xo[i][0] = *reinterpret_cast<const double2 *>(xp);
-                    xo[i][1] = *reinterpret_cast<const double2 *>(xp + 2);
-                    ro[i][0] = *reinterpret_cast<const double2 *>(rp);
-                    ro[i][1] = *reinterpret_cast<const double2 *>(rp + 2);
+                if constexpr (FF) {
+                    xhv[i] = xlv[i] = rhv[i] = rlv[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (row < n) {
+                        const int64_t e = row * 16 + 4 * c4;
+                        xhv[i] = *reinterpret_cast<const float4 *>(Xh + e);
+                        xlv[i] = *reinterpret_cast<const float4 *>(Xl + e);
+                        rhv[i] = *reinterpret_cast<const float4 *>(Rh + e);
+                        rlv[i] = *reinterpret_cast<const float4 *>(Rl + e);
+                    }
+                } else {
+                    xo[i][0] = xo[i][1] = ro[i][0] = ro[i][1] = make_double2(0.0, 0.0);
+                    if (row < n) {
+                        const double *xp = X + row * 16 + 4 * c4, *rp = R + row * 16 + 4 * c4;
+                        xo[i][0] = *reinterpret_cast<const double2 *>(xp);
+                        xo[i][1] = *reinterpret_cast<const double2 *>(xp + 2);
+                        ro[i][0] = *reinterpret_cast<const double2 *>(rp);
+                        ro[i][1] = *reinterpret_cast<const double2 *>(rp + 2);
+                    }
                 }
             }
             const bool w = t5_mbar_wait_or_abort(&full[q], qph, abort_flag);
@@ -313,8 +346,7 @@ __global__ void __launch_bounds__(kXtThreads, 1)
                     }
                 }
             }
-            __syncwarp();
-            if (lane == 0) t5_mbar_arrive(&empty[q]);  // this warp's rows of the stage are read
+            const int qdone = q;
             if (++q == stages) {
                 q = 0;
                 qph ^= 1u;
@@ -323,6 +355,27 @@ __global__ void __launch_bounds__(kXtThreads, 1)
             for (int i = 0; i < RPT; ++i) {
                 const int64_t row = row0 + kXtSlots * i;
                 if (row >= n) break;
+                if constexpr (FF) {
+                    float xh[4] = {xhv[i].x, xhv[i].y, xhv[i].z, xhv[i].w};
+                    float xl[4] = {xlv[i].x, xlv[i].y, xlv[i].z, xlv[i].w};
+                    float rh[4] = {rhv[i].x, rhv[i].y, rhv[i].z, rhv[i].w};
+                    float rl[4] = {rlv[i].x, rlv[i].y, rlv[i].z, rlv[i].w};
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        ff_add_float(xh[c], xl[c], ax[i][c]);
+                        ff_add_float(rh[c], rl[c], -ar[i][c]);
+                        ff_add_square(rh[c], rl[c], sq_hi[c], sq_lo[c]);
+                    }
+                    const int64_t e = row * 16 + 4 * c4;
+                    *reinterpret_cast<float4 *>(Xh + e) = make_float4(xh[0], xh[1], xh[2], xh[3]);
+                    *reinterpret_cast<float4 *>(Xl + e) = make_float4(xl[0], xl[1], xl[2], xl[3]);
+                    const float4 r4 = make_float4(rh[0], rh[1], rh[2], rh[3]);
+                    *reinterpret_cast<float4 *>(Rh + e) = r4;
+                    *reinterpret_cast<float4 *>(Rl + e) = make_float4(rl[0], rl[1], rl[2], rl[3]);
+                    if (S0) *reinterpret_cast<float4 *>(S0 + row * lds + 4 * c4) = r4;
+                    if (R32) *reinterpret_cast<float4 *>(R32 + e) = r4;
+                    continue;
+                }
                 const double xv[4] = {xo[i][0].x, xo[i][0].y, xo[i][1].x, xo[i][1].y};
                 const double rv[4] = {ro[i][0].x, ro[i][0].y, ro[i][1].x, ro[i][1].y};
                 double xn[4], rn[4];
@@ -345,6 +398,13 @@ __global__ void __launch_bounds__(kXtThreads, 1)
                 if (S0) *reinterpret_cast<float4 *>(S0 + row * lds + 4 * c4) = r4;
                 if (R32) *reinterpret_cast<float4 *>(R32 + row * 16 + 4 * c4) = r4;
             }
+            // every thread releases its own reads of the stage, after the
+            // epilogue and behind a proxy fence: released right after the FMA
+            // loop by lane 0 (after __syncwarp), the next TMA fill overwrote
+            // rows whose shared-memory loads had not completed (seen as
+            // run-to-run differences in a few rows of a tile)
+            t5_fence_proxy_async();
+            t5_mbar_arrive(&empty[qdone]);
         }
         if (!ok && lane == 0) fail();
 #pragma unroll
@@ -358,9 +418,9 @@ __global__ void __launch_bounds__(kXtThreads, 1)
     }
 }
 
-template <int NBX>
+template <int NBX, bool FF>
 int launch_xt(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ, int64_t ldq,
-              const double *alpha, double *X, double *R, float *S0, int64_t lds, float *R32,
+              const double *alpha, void *X, void *R, float *S0, int64_t lds, float *R32,
               double *norms, double *ws, int *status) {
     constexpr int kXtRows = kXtSlots * kXtRpt;
     const size_t budget = (size_t)max_smem_optin();
@@ -375,7 +435,7 @@ int launch_xt(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ
                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B))
         return CACG_ERR_UNSUPPORTED;
     static const bool attr = [] {
-        cudaFuncSetAttribute(xrupdate16_tma_kernel<NBX>,
+        cudaFuncSetAttribute(xrupdate16_tma_kernel<NBX, FF>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem_optin());
         return true;
     }();
@@ -383,7 +443,7 @@ int launch_xt(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ
     const int64_t ntiles = (n + kXtRows - 1) / kXtRows;
     const int grid =
         (int)std::min<int64_t>(ntiles, std::min<int64_t>(sm_count(), kXr16MaxBlocks));
-    xrupdate16_tma_kernel<NBX><<<grid, kXtThreads, smem, st>>>(
+    xrupdate16_tma_kernel<NBX, FF><<<grid, kXtThreads, smem, st>>>(
         mq, ma, n, k, stages, alpha, X, R, S0, lds, R32, norms ? ws : nullptr, status);
     int rc = check_launch();
     if (rc != CACG_OK || !norms) return rc;
@@ -394,9 +454,9 @@ bool a16(const void *p) { return ((uintptr_t)p & 15) == 0; }
 
 }  // namespace
 
-int launch_xrupdate_m16_tma(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
-                            int64_t ldq, const double *alpha, double *X, double *R, float *S0,
-                            int64_t lds, float *R32, double *norms, double *ws, int *status) {
+static int launch_xt_any(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
+                        int64_t ldq, const double *alpha, void *X, void *R, float *S0,
+                        int64_t lds, float *R32, double *norms, double *ws, int *status, bool ff) {
     if (k <= 0 || k % 4 != 0 || k > 128 || ldq % 4 || !a16(Q) || !a16(AQ) || !a16(X) ||
         !a16(R) || !status)
         return CACG_ERR_UNSUPPORTED;
@@ -404,13 +464,34 @@ int launch_xrupdate_m16_tma(cudaStream_t st, int64_t n, int k, const float *Q, c
     if (R32 && !a16(R32)) return CACG_ERR_UNSUPPORTED;
     if (norms && !ws) return CACG_ERR_ARG;
     if (n <= 0) return CACG_ERR_UNSUPPORTED;
+#define XT_CASE(B)                                                                               \
+    case B:                                                                                      \
+        return ff ? launch_xt<B, true>(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms,  \
+                                       ws, status)                                              \
+                  : launch_xt<B, false>(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms, \
+                                        ws, status);
     switch ((k + 31) / 32) {
-        case 1: return launch_xt<1>(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms, ws, status);
-        case 2: return launch_xt<2>(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms, ws, status);
-        case 3: return launch_xt<3>(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms, ws, status);
-        case 4: return launch_xt<4>(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms, ws, status);
+        XT_CASE(1)
+        XT_CASE(2)
+        XT_CASE(3)
+        XT_CASE(4)
     }
+#undef XT_CASE
     return CACG_ERR_UNSUPPORTED;
+}
+
+int launch_xrupdate_m16_tma(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
+                            int64_t ldq, const double *alpha, double *X, double *R, float *S0,
+                            int64_t lds, float *R32, double *norms, double *ws, int *status) {
+    return launch_xt_any(st, n, k, Q, AQ, ldq, alpha, X, R, S0, lds, R32, norms, ws, status,
+                         false);
+}
+
+int launch_xrupdate_m16_ff(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,
+                           int64_t ldq, const double *alpha, float *Xff, float *Rff, float *S0,
+                           int64_t lds, float *R32, double *norms, double *ws, int *status) {
+    return launch_xt_any(st, n, k, Q, AQ, ldq, alpha, Xff, Rff, S0, lds, R32, norms, ws, status,
+                         true);
 }
 
 int launch_xrupdate_m16(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ,

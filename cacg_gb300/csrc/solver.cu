@@ -150,8 +150,8 @@ void DevMatrix::release() {
 static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct Layout {
-    size_t S, Q, AQ, R, R32, Xff, Bnorm, small, gram, norm, lanczos, total;
-    size_t o_S, o_Q, o_AQ, o_R, o_R32, o_Xff, o_small, o_gram, o_norm, o_lanczos;
+    size_t S, Q, AQ, R, R32, Xff, Rff, Bnorm, small, gram, norm, lanczos, total;
+    size_t o_S, o_Q, o_AQ, o_R, o_R32, o_Xff, o_Rff, o_small, o_gram, o_norm, o_lanczos;
     size_t Ssl, R32sl, o_Ssl, o_Qsl, o_AQsl, o_R32sl;
     bool slices;
 };
@@ -174,6 +174,7 @@ static Layout layout(int64_t n, int m, int s, int prec, bool lanczos, bool slice
     L.R = align256((size_t)n * m * 8);
     L.R32 = prec == CACG_MIXED ? align256((size_t)n * m * 4) : 0;
     L.Xff = prec == CACG_MIXED ? align256((size_t)n * m * 8) : 0;  // X as FP32 hi, lo
+    L.Rff = prec == CACG_MIXED ? align256((size_t)n * m * 8) : 0;  // R as FP32 hi, lo
     L.Ssl = slices ? align256((size_t)3 * n * k * 2) : 0;
     L.R32sl = slices ? align256((size_t)3 * n * m * 2) : 0;
     // small: QtAS k*k, QtAQ k*k, QtR k*m, F 2*k*k + k, alpha k*m, beta k*k, norms m,
@@ -195,6 +196,7 @@ static Layout layout(int64_t n, int m, int s, int prec, bool lanczos, bool slice
     L.o_R = o; o += L.R;
     L.o_R32 = o; o += L.R32;
     L.o_Xff = o; o += L.Xff;
+    L.o_Rff = o; o += L.Rff;
     L.o_small = o; o += L.small;
     L.o_gram = o; o += L.gram;
     L.o_norm = o; o += L.norm;
@@ -432,6 +434,7 @@ struct SolveBuffers {
     double *norm_ws;
     int64_t norm_ws_doubles;
     float *Xff;  // n x m hi, then n x m lo (mixed mode's float-float residual)
+    float *Rff;  // the same for R (the float-float state of the mixed mode)
     double *lz;  // 3 x n (Lanczos)
     Slices Ssl, Qsl, AQsl, R32sl;  // bf16 slice planes (mixed mode, when enabled)
 };
@@ -443,6 +446,7 @@ static void carve(char *base, const Layout &L, int m, int k, SolveBuffers *b) {
     b->R = (double *)(base + L.o_R);
     b->R32 = L.R32 ? (float *)(base + L.o_R32) : nullptr;
     b->Xff = L.Xff ? (float *)(base + L.o_Xff) : nullptr;
+    b->Rff = L.Rff ? (float *)(base + L.o_Rff) : nullptr;
     double *sm = (double *)(base + L.o_small);
     b->QtAS = sm; sm += (size_t)k * k;
     b->QtAQ = sm; sm += (size_t)k * k;
@@ -635,6 +639,9 @@ struct Solver {
     // the X whose FP64 residual b.R holds (nullptr once X may have changed):
     // the final true residual then needs only its norms
     const double *r_fp64_of = nullptr;
+    // float-float state (mixed mode, m = 16, DIA view): X and R live in Xff,
+    // Rff between FP64 checks; x_dirty: the FP64 X lags Xff
+    bool ffx = false, x_dirty = false, xff_valid = false;
 
     // R = B - A X.  ff: in the mixed mode over a DIA view, float-float
     // arithmetic (FP32 pipe) instead of FP64 -- used for the periodic residual
@@ -651,14 +658,31 @@ struct Solver {
                    2.0 * (double)A->nnz * m);
         int rc;
         if (ff) {
-            rc = launch_dia_residual_ff(st, A, m, X, B, R, b.Xff, b.Xff + (size_t)A->n * m,
+            // on the float-float state X is already split and R goes to Rff
+            rc = launch_dia_residual_ff(st, A, m, ffx && xff_valid ? nullptr : X, B,
+                                        ffx ? nullptr : R, b.Xff, b.Xff + (size_t)A->n * m,
                                         write_s0 ? (float *)b.S : nullptr, k,
                                         write_s0 ? b.R32 : nullptr, norms, b.norm_ws,
-                                        b.norm_ws_doubles);
+                                        b.norm_ws_doubles, ffx ? b.Rff : nullptr);
             if (rc != CACG_ERR_UNSUPPORTED) {
+                if (rc == CACG_OK && ffx) xff_valid = true;
                 prof.end();
                 return rc;
             }
+            if (ffx && xff_valid) {
+                prof.end();
+                return CACG_ERR_CUDA;  // the float-float state cannot leave the ff kernels
+            }
+            ffx = false;  // not supported for this matrix: FP64 state from the start
+        }
+        if (ffx && x_dirty) {  // an FP64 residual of the float-float X
+            rc = launch_ff_join(st, A->n * (int64_t)m, b.Xff, b.Xff + (size_t)A->n * m,
+                                const_cast<double *>(X));
+            if (rc) {
+                prof.end();
+                return rc;
+            }
+            x_dirty = false;
         }
         if (slices && write_s0) {
             rc = launch_residual_sl(st, A->n, A->rp, A->ci, A->val, m, X, B, R, (float *)b.S, k,
@@ -670,6 +694,9 @@ struct Solver {
                                           prec == CACG_MIXED, k, norms, b.norm_ws);
             if (rc == CACG_OK && write_s0 && b.R32)
                 rc = launch_cast_f64_f32(st, A->n * m, R, b.R32);
+            // the iterations continue from this R on the float-float state
+            if (rc == CACG_OK && ffx && R == b.R)
+                rc = launch_ff_split(st, A->n * (int64_t)m, R, b.Rff, b.Rff + (size_t)A->n * m);
             if (rc == CACG_OK && R == b.R) r_fp64_of = X;
         }
         prof.end();
@@ -827,6 +854,10 @@ struct Solver {
         // (the tcgen05 X/R update, launch_xrupdate_tc5, is slower than the
         // CUDA-core kernels at m = 16: its N = 16 MMAs are latency-bound)
         if constexpr (std::is_same<T, float>::value) {
+            if (ffx)
+                return launch_xrupdate_m16_ff(st, A->n, k, Q, AQ, k, b.alpha, b.Xff, b.Rff,
+                                              (float *)b.S, k, b.R32, b.norms, b.norm_ws,
+                                              b.status);
             if (m == 16) {
                 int rc = launch_xrupdate_m16_tma(st, A->n, k, Q, AQ, k, b.alpha, X, b.R,
                                                  (float *)b.S, k, b.R32, b.norms, b.norm_ws,
@@ -877,6 +908,12 @@ struct Solver {
             CACG_CUDA_TRY(cudaStreamSynchronize(st));
             for (int c = 0; c < m; ++c) bn[c] = h_pin[c] > 0 ? sqrt(h_pin[c]) : 1.0;
         }
+        // float-float state for the mixed mode's 16-column blocks over a DIA view
+        xff_valid = false;
+        x_dirty = false;
+        ffx = prec == CACG_MIXED && m == 16 && uses_dia() && !slices && b.Xff && b.Rff &&
+              A->dia32 && A->dia32lo && p.residual_precision != CACG_RESID_FP64 &&
+              !p.exact_updates && k % 4 == 0 && k <= 128 && n < (int64_t)INT32_MAX - 256;
         rc = residual(B, X, b.R, true, b.norms, true);
         if (rc) return rc;
 
@@ -904,6 +941,7 @@ struct Solver {
         const bool prof_on = prof.on;
         for (it = 0; it < p.maxit; ++it) {
             r_fp64_of = nullptr;  // this iteration updates X
+            if (ffx) x_dirty = true;  // (in Xff; the FP64 X is joined on demand)
             if (graphs && it >= 2) {
                 const int par = it & 1;
                 prof.on = false;
@@ -974,6 +1012,12 @@ struct Solver {
                     break;
                 }
             }
+        }
+        // the float-float X back to FP64 (the caller's X)
+        if (ffx && x_dirty) {
+            rc = launch_ff_join(st, n * (int64_t)m, b.Xff, b.Xff + (size_t)n * m, X);
+            if (rc) return rc;
+            x_dirty = false;
         }
         // final true residual per column (FP64); after a converged FP64 check
         // b.R already holds B - A X for this X

@@ -88,6 +88,10 @@ extern "C" {
                             k <= 256, m <= 16 dividing 32; both: 16-byte aligned rows */
 #define CACG_VAL_TC5_CPASYNC 64 /* with CACG_VAL_TC5 in cacg_k_qupdate: the cp.async-fed
                                    kernel instead of the TMA-fed one (bit-identical) */
+#define CACG_XR_FFSTATE 128 /* or-ed into cacg_k_xrupdate's vtype (FP32, m = 16): X and R
+                               are float-float pairs, each n x 16 FP32 high parts followed
+                               by n x 16 low parts (the byte size of n x 16 doubles) -- the
+                               mixed solve's state; S0 = R32 = the high part of R */
 
 /* generators (cacg_gen_*) */
 #define CACG_GEN_LAPLACE2D_5PT 1

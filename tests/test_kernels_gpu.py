@@ -304,6 +304,56 @@ def test_xrupdate_m16_tma(lib, torch_cuda, n, k):
     assert relerr(host(norms), (Rg * Rg).sum(axis=0)) <= 1e-13
 
 
+FFSTATE = 128
+
+
+@pytest.mark.parametrize("n,k", [(130001, 96), (999, 48), (300000, 96)])
+def test_xrupdate_ffstate_matches_fp64(lib, torch_cuda, n, k):
+    """X and R as float-float pairs (the mixed solve's state): the same update
+    as the FP64-state kernel to the pairs' precision (about 2^-48), the same
+    S0 and norms to FP32 rounding, and bit-identical on repeated calls."""
+    torch = torch_cuda
+    m = 16
+    Q = O.gen_rhs("normal", n, k, 31).astype(np.float32)
+    AQ = O.gen_rhs("normal", n, k, 32).astype(np.float32)
+    al = O.gen_rhs("normal", k, m, 33)
+    X0 = O.gen_rhs("normal", n, m, 34)
+    R0 = O.gen_rhs("normal", n, m, 35)
+    dQ, dAQ, dal = dev(torch, Q), dev(torch, AQ), dev(torch, al)
+
+    # FP64 state
+    dX, dR = dev(torch, X0), dev(torch, R0)
+    S0a = torch.zeros((n, k), dtype=torch.float32, device="cuda")
+    na = torch.zeros(m, dtype=torch.float64, device="cuda")
+    assert lib.cacg_k_xrupdate(F32, n, k, m, ptr(dQ), ptr(dAQ), k, ptr(dal), ptr(dX), ptr(dR),
+                               ptr(S0a), k, ptr(na), None) == 0
+    X1, R1 = host(dX), host(dR)
+
+    def pair(x):
+        hi = x.astype(np.float32)
+        lo = (x - hi.astype(np.float64)).astype(np.float32)
+        return np.concatenate([hi.ravel(), lo.ravel()])
+
+    def join(p):
+        return p[:n * m].astype(np.float64).reshape(n, m) + p[n * m:].astype(np.float64).reshape(n, m)
+
+    outs = []
+    for _ in range(3):
+        px, pr = dev(torch, pair(X0)), dev(torch, pair(R0))
+        S0b = torch.zeros((n, k), dtype=torch.float32, device="cuda")
+        nb = torch.zeros(m, dtype=torch.float64, device="cuda")
+        assert lib.cacg_k_xrupdate(F32 | FFSTATE, n, k, m, ptr(dQ), ptr(dAQ), k, ptr(dal),
+                                   ptr(px), ptr(pr), ptr(S0b), k, ptr(nb), None) == 0
+        outs.append((host(px), host(pr), host(S0b), host(nb)))
+    for o in outs[1:]:
+        assert all(np.array_equal(a, b) for a, b in zip(outs[0], o))
+    px, pr, S0b, nb = outs[0]
+    assert relerr(join(px), X1) <= 1e-13
+    assert relerr(join(pr), R1) <= 1e-13
+    assert np.max(np.abs(S0b[:, :m] - host(S0a)[:, :m])) <= 2e-7 * np.max(np.abs(R1))
+    assert relerr(nb, host(na)) <= 1e-12
+
+
 @pytest.mark.parametrize("n,k,m", [(10000, 64, 8), (20000, 96, 16), (777, 4, 1),
                                    (3000, 20, 4), (4000, 256, 16), (130001, 96, 16),
                                    (5001, 32, 2)])
