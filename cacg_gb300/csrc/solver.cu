@@ -966,20 +966,21 @@ struct Solver {
             ++since_rr;
             res->iterations = it + 1;
             res->recurrence_norm0 = sqrt(std::max(h_pin[0], 0.0));
-            if (stv & kStatusTimeout) {
-                res->status = CACG_ERR_TIMEOUT;
-                return CACG_ERR_TIMEOUT;
-            }
-            if (stv & kStatusBreakdown) {
-                res->status = CACG_ERR_BREAKDOWN;
-                return CACG_ERR_BREAKDOWN;
-            }
+            // an early stop leaves the caller's X at the last iterate, as the
+            // FP64 state does (the float-float X is joined back first)
+            auto stop = [&](int code) {
+                if (ffx && x_dirty &&
+                    launch_ff_join(st, n * (int64_t)m, b.Xff, b.Xff + (size_t)n * m, X) ==
+                        CACG_OK)
+                    cudaStreamSynchronize(st);
+                res->status = code;
+                return code;
+            };
+            if (stv & kStatusTimeout) return stop(CACG_ERR_TIMEOUT);
+            if (stv & kStatusBreakdown) return stop(CACG_ERR_BREAKDOWN);
             bool finite = true;
             for (int c = 0; c < m; ++c) finite = finite && std::isfinite(h_pin[c]);
-            if (!finite) {
-                res->status = CACG_ERR_BREAKDOWN;
-                return CACG_ERR_BREAKDOWN;
-            }
+            if (!finite) return stop(CACG_ERR_BREAKDOWN);
             if (p.tol_mode == CACG_TOL_ABS_COL0) {
                 // the reference's test, src/bcbcgKernel.c:524
                 if (sqrt(h_pin[0]) < p.tol) {
