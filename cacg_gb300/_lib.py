@@ -23,6 +23,8 @@ SPMM_AUTO, SPMM_CSR, SPMM_DIA_UNSTAGED = 0, 1, 2
 ALG_CACG, ALG_BCG = 0, 1
 RESID_AUTO, RESID_FP64 = 0, 1
 VAL_F64, VAL_F32 = 0, 1
+# or-ed into the vtype of the kernel entry points (cacg_k_qupdate / cacg_k_xrupdate)
+XR_EXACT, VAL_TC5, VAL_TC5_CPASYNC, XR_FFSTATE = 16, 32, 64, 128
 
 
 class CacgCsr(C.Structure):

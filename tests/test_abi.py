@@ -53,6 +53,21 @@ def _c_layout(structs):
     return dict(line.split() for line in out.splitlines())
 
 
+def test_python_constants_match_header_defines():
+    """Every integer #define CACG_<NAME> of include/cacg.h that the ctypes
+    mirror also names (<NAME>) has the same value there."""
+    text = open(os.path.join(INC, "cacg.h")).read()
+    defines = {m.group(1): int(m.group(2))
+               for m in re.finditer(r"^#define\s+CACG_(\w+)\s+(-?\d+)", text, flags=re.M)}
+    shared = [k for k in defines if hasattr(L, k)]
+    for k in ("VAL_F64", "VAL_F32", "XR_EXACT", "VAL_TC5", "VAL_TC5_CPASYNC", "XR_FFSTATE",
+              "SPMM_AUTO", "SPMM_CSR", "SPMM_DIA_UNSTAGED", "ALG_CACG", "ALG_BCG", "GRAM_TC5",
+              "MIXED", "FP64"):
+        assert k in shared, k
+    for k in shared:
+        assert getattr(L, k) == defines[k], (k, getattr(L, k), defines[k])
+
+
 def test_struct_layouts_match_header():
     py = {"cacg_params": L.CacgParams, "cacg_result": L.CacgResult, "cacg_csr": L.CacgCsr,
           "csrType_local": L.CsrTypeLocal, "denseType": L.DenseType,
