@@ -161,8 +161,10 @@ __global__ void __launch_bounds__(kXr16Threads)
 // Q and AQ rows (swizzled positions: the eight rows a warp reads at once hit
 // distinct banks) and four alpha rows (FP32, broadcast); the FMAs go out as
 // packed pairs (fma.rn.f32x2), summing over k in increasing order.
-// X and R (128-byte FP64 rows) are read with coalesced loads issued before
-// the stage wait, and the epilogue is that of xrupdate16_kernel.
+// X and R rows are read with coalesced loads issued before the stage wait:
+// FP64 rows (the epilogue of xrupdate16_kernel), or float-float pairs (FF:
+// the additions in float-float, no FP64 instruction).  Every compute thread
+// releases the stage after its epilogue, behind a proxy fence.
 constexpr int kXtWarps = 8;                       // compute warps
 constexpr int kXtSlots = 8 * kXtWarps;            // row slots (a thread's first row)
 constexpr int kXtThreads = 32 * (kXtWarps + 1);   // + the loader warp
