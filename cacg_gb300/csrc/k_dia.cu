@@ -604,7 +604,9 @@ __global__ void __launch_bounds__(kDiaThreads, 2)
 // (two columns per instruction: mul/fma/add/sub .rn.f32x2).  Every pair lane
 // computes exactly what ff_mac computes for its column -- the product is
 // formed as -p = (-a) x so that e = fma(a, x, -p) needs no negation -- so the
-// result is bit-identical to dia_resid_ff_kernel.
+// FP64 R, S0, R32 and norms are bit-identical to dia_resid_ff_kernel's.  With
+// Rff the kernel writes R as a normalised float-float pair instead (the
+// mixed solve's float-float state) and sums the norms in float-float.
 __device__ __forceinline__ unsigned long long ff_pack(float lo, float hi) {
     unsigned long long r;
     asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
