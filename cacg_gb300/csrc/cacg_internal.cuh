@@ -46,6 +46,15 @@ inline int check_launch() {
 int sm_count();              // multiprocessors of the current device
 size_t max_smem_optin();     // opt-in shared memory per block (bytes)
 
+// Opt-in dynamic shared memory of a kernel, set on the current device the
+// first time that device launches it (the attribute belongs to the device's
+// context: a process that drives several devices sets it on each).
+void set_smem_attr_fn(const void *fn, int bytes);
+template <typename K>
+inline void set_smem_attr(K *fn, int bytes) {
+    set_smem_attr_fn(reinterpret_cast<const void *>(fn), bytes);
+}
+
 // ------------------------------------------------------- vector traits
 template <typename T> struct Vec16;
 template <> struct Vec16<double> {

@@ -420,12 +420,7 @@ static int launch_dia_kernel(cudaStream_t st, const DevMatrix *A, const T *vals,
     const int BR = runs_per_block * R;
     const size_t smem = R > 1 ? 2 * (size_t)A->dia_ndiag * BR * sizeof(T) : 0;
     if (smem > 200 * 1024) return CACG_ERR_UNSUPPORTED;
-    static const bool attr = [] {
-        cudaFuncSetAttribute(dia_spmm_kernel<T, R, CW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             200 * 1024);
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(dia_spmm_kernel<T, R, CW>, 200 * 1024);
     const int64_t nblk = (A->n + BR - 1) / BR;
     int per_sm = 2;
     if (smem > 0) per_sm = std::max(1, std::min(R <= 4 ? 4 : 2, (int)(220 * 1024 / smem)));
@@ -834,14 +829,8 @@ int launch_dia_residual_ff(cudaStream_t st, const DevMatrix *A, int m, const dou
     // X == NULL: Xh, Xl already hold X
     int rc = X ? launch_ff_split(st, A->n * (int64_t)m, X, Xh, Xl) : CACG_OK;
     if (rc != CACG_OK) return rc;
-    static const bool attr = [] {
-        cudaFuncSetAttribute(dia_resid_ff_kernel<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             200 * 1024);
-        cudaFuncSetAttribute(dia_resid_ff16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             200 * 1024);
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(dia_resid_ff_kernel<RR>, 200 * 1024);
+    set_smem_attr(dia_resid_ff16_kernel, 200 * 1024);
     if (k16) {
         dia_resid_ff16_kernel<<<(unsigned)blocks, kDiaThreads, smem, st>>>(
             A->n, A->dia_npad, A->dia, A->dia32, Xh, Xl, B, Rff ? nullptr : R, Rff, S0, lds, R32,

@@ -379,12 +379,7 @@ int ring_launch(cudaStream_t st, const CUtensorMap &tmx, const CUtensorMap &tmm,
                 const CUtensorMap &tmv, int64_t n, const DiaDesc &desc, RingDesc &rd, size_t smem,
                 float *Y, int64_t ldy, const float *Z1, int64_t ldz1, const float *Z2, int64_t ldz2,
                 float ca, float cb, float cc, int *status) {
-    static const bool attr = [] {
-        cudaFuncSetAttribute(dia_ring_kernel<NB, GPB, G>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, kRingSmemMax);
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(dia_ring_kernel<NB, GPB, G>, kRingSmemMax);
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dia_ring_kernel<NB, GPB, G>,
                                                       kRingThreads + 32, smem) != cudaSuccess ||

@@ -152,12 +152,7 @@ int launch_wide(cudaStream_t st, const DevMatrix *A, const float *X, float *Y, f
     constexpr int BR = (kWideThreads / (COLS / 4)) * kWideR;
     const size_t smem = 2 * (size_t)A->dia_ndiag * BR * sizeof(float);
     if (smem > 96 * 1024) return CACG_ERR_UNSUPPORTED;
-    static const bool attr = [] {
-        cudaFuncSetAttribute(dia_wide_kernel<COLS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             96 * 1024);
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(dia_wide_kernel<COLS>, 96 * 1024);
     const int64_t nblk = (A->n + BR - 1) / BR;
     const int64_t blocks = std::min<int64_t>(nblk, (int64_t)sm_count() * kWideCtas);
     dia_wide_kernel<COLS><<<(unsigned)blocks, kWideThreads, smem, st>>>(

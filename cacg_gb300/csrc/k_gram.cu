@@ -395,6 +395,8 @@ int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl
                 double *C1, int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes) {
     const int kb = kb1 + kb2;
     if (ka <= 0 || kb <= 0 || n < 0 || !C1 || (kb2 > 0 && !C2)) return CACG_ERR_ARG;
+    if (variant != CACG_GRAM_AUTO && variant != CACG_GRAM_FMA && variant != CACG_GRAM_DMMA)
+        return CACG_ERR_UNSUPPORTED;
     if (variant == CACG_GRAM_AUTO) variant = CACG_GRAM_FMA;
     if (!std::is_same<T, double>::value) variant = CACG_GRAM_FMA;
     if (variant == CACG_GRAM_DMMA) {
@@ -409,26 +411,14 @@ int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl
     if (n > 0) {
         if (variant == CACG_GRAM_DMMA) {
             if constexpr (std::is_same<T, double>::value) {
-                static const bool attr = [] {
-                    cudaFuncSetAttribute(gram_dmma_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)max_smem_optin());
-                    return true;
-                }();
-                (void)attr;
+                set_smem_attr(gram_dmma_kernel, (int)max_smem_optin());
                 gram_dmma_kernel<<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl,
                                                                   ka, R1, ldr1, kb1, R2, ldr2,
                                                                   kb2, p.BA, p.BB, p.tilesB,
                                                                   ws);
             }
         } else {
-            static const bool attr = [] {
-                cudaFuncSetAttribute(gram_fma_kernel<T>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)max_smem_optin());
-                return true;
-            }();
-            (void)attr;
+            set_smem_attr(gram_fma_kernel<T>, (int)max_smem_optin());
             gram_fma_kernel<T><<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl,
                                                                 ka, R1, ldr1, kb1, R2, ldr2,
                                                                 kb2, p.BA, p.BB, p.tilesB, ws);
@@ -570,9 +560,17 @@ extern "C" int cacg_k_gram(int32_t vtype, int32_t variant, int64_t n, const void
 //   race on the array: serialise them.
 // * Device addresses: the host-side name of the array is not a device
 //   address.  The first call on each device (that device current) looks the
-//   address up once with cudaGetSymbolAddress and caches it; make that first
-//   call before any stream capture.
+//   address up once with cudaGetSymbolAddress and caches it under the
+//   device's current context ID, so a context re-created after
+//   cudaDeviceReset gets a fresh lookup; make the first call in each context
+//   before any stream capture.
+// * variant: CACG_GRAM_AUTO, CACG_GRAM_FMA or CACG_GRAM_DMMA (FP64 inputs);
+//   the tensor-core variants of cacg_k_gram need their own workspace and are
+//   refused with CACG_ERR_UNSUPPORTED.  FP32 inputs take the FP64-accurate
+//   CUDA-core product whatever the variant.
 // ---------------------------------------------------------------------------
+#include <cuda.h>
+
 #include <cstdio>
 #include <mutex>
 
@@ -583,7 +581,41 @@ static __device__ __align__(256) double
     g_gram_noalloc_scratch[kGramNoAllocScratchBytes / sizeof(double)];
 
 static std::mutex g_noalloc_mu;
-static double *g_noalloc_ptr[64];
+struct NoAllocEntry {
+    unsigned long long ctx_id;  // 0: not looked up yet
+    double *ptr;
+};
+static NoAllocEntry g_noalloc[64];
+
+// ID of the current context (unique for the process's lifetime, unlike the
+// context handle); 0 when the driver does not provide it.
+static unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr, *q = nullptr;
+        cudaDriverEntryPointQueryResult r1 = cudaDriverEntryPointSymbolNotFound, r2 = r1;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault,
+                                             &r1) == cudaSuccess &&
+            r1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &q, 12000, cudaEnableDefault, &r2) ==
+                cudaSuccess &&
+            r2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<GetCurrent>(p);
+            get_id = reinterpret_cast<GetId>(q);
+        }
+        cudaGetLastError();
+    });
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c ||
+        get_id(c, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 static int noalloc_scratch(double **out) {
     int dev = 0;
@@ -591,19 +623,29 @@ static int noalloc_scratch(double **out) {
         cudaGetLastError();
         return CACG_ERR_CUDA;
     }
+    // cudaSetDevice initialises the device's primary context and makes it
+    // current on this thread, so the context ID below is the one the kernels
+    // will run in
+    if (cudaSetDevice(dev) != cudaSuccess) {
+        cudaGetLastError();
+        return CACG_ERR_CUDA;
+    }
+    const unsigned long long id = current_context_id();
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    NoAllocEntry &e = g_noalloc[dev];
+    if (id == 0 || e.ctx_id != id) {
         double *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_gram_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            record_cuda_error(e, "cudaGetSymbolAddress(g_gram_noalloc_scratch)", __FILE__,
+        cudaError_t rc = cudaGetSymbolAddress((void **)&p, g_gram_noalloc_scratch);
+        if (rc != cudaSuccess || !p) {
+            record_cuda_error(rc, "cudaGetSymbolAddress(g_gram_noalloc_scratch)", __FILE__,
                               __LINE__);
             cudaGetLastError();
             return CACG_ERR_CUDA;
         }
-        g_noalloc_ptr[dev] = p;
+        e.ctx_id = id;
+        e.ptr = p;
     }
-    *out = g_noalloc_ptr[dev];
+    *out = e.ptr;
     return CACG_OK;
 }
 
@@ -614,6 +656,8 @@ static int gram_fixed_scratch(cudaStream_t st, int variant, int64_t n, const T *
                               double *ws, size_t ws_bytes) {
     const int kb = kb1 + kb2;
     if (ka <= 0 || kb <= 0 || n < 0 || !C1 || (kb2 > 0 && !C2)) return CACG_ERR_ARG;
+    if (variant != CACG_GRAM_AUTO && variant != CACG_GRAM_FMA && variant != CACG_GRAM_DMMA)
+        return CACG_ERR_UNSUPPORTED;
     if (variant == CACG_GRAM_AUTO) variant = CACG_GRAM_FMA;
     if (!std::is_same<T, double>::value) variant = CACG_GRAM_FMA;
     if (variant == CACG_GRAM_DMMA) {
@@ -642,26 +686,14 @@ static int gram_fixed_scratch(cudaStream_t st, int variant, int64_t n, const T *
     if (n > 0) {
         if (variant == CACG_GRAM_DMMA) {
             if constexpr (std::is_same<T, double>::value) {
-                static const bool attr = [] {
-                    cudaFuncSetAttribute(gram_dmma_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)max_smem_optin());
-                    return true;
-                }();
-                (void)attr;
+                set_smem_attr(gram_dmma_kernel, (int)max_smem_optin());
                 gram_dmma_kernel<<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl,
                                                                   ka, R1, ldr1, kb1, R2, ldr2,
                                                                   kb2, p.BA, p.BB, p.tilesB,
                                                                   ws);
             }
         } else {
-            static const bool attr = [] {
-                cudaFuncSetAttribute(gram_fma_kernel<T>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)max_smem_optin());
-                return true;
-            }();
-            (void)attr;
+            set_smem_attr(gram_fma_kernel<T>, (int)max_smem_optin());
             gram_fma_kernel<T><<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl,
                                                                 ka, R1, ldr1, kb1, R2, ldr2,
                                                                 kb2, p.BA, p.BB, p.tilesB, ws);

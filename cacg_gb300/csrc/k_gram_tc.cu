@@ -336,12 +336,7 @@ int launch_gram_tc(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int 
                       (ka % 4 == 0) && (kb1 % 4 == 0) && (kb2 % 4 == 0) && aligned16(L) &&
                       aligned16(R1) && (kb2 == 0 || aligned16(R2));
     if (n > 0) {
-        static const bool attr = [] {
-            cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)max_smem_optin());
-            return true;
-        }();
-        (void)attr;
+        set_smem_attr(gram_tc_kernel, (int)max_smem_optin());
         dim3 grid(p.nchunks, p.tilesA * p.tilesB);
         gram_tc_kernel<<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl, ka, R1, ldr1,
                                                         kb1, R2, ldr2, kb2, p.BA, p.BB, p.tilesB,
@@ -582,14 +577,8 @@ int launch_gram_tcs(cudaStream_t st, int64_t n, Slices L, int64_t ldl, int ka, S
     const size_t need = (size_t)p.nchunks * p.tilesA * p.tilesB * p.BA * p.BB * sizeof(double);
     if (!ws || need > ws_bytes || p.threads > kTcMaxThreads) return CACG_ERR_ARG;
     if (n > 0) {
-        static const bool attr = [] {
-            cudaFuncSetAttribute(gram_tcs_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)max_smem_optin());
-            cudaFuncSetAttribute(gram_tcs_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)max_smem_optin());
-            return true;
-        }();
-        (void)attr;
+        set_smem_attr(gram_tcs_kernel<2>, (int)max_smem_optin());
+        set_smem_attr(gram_tcs_kernel<3>, (int)max_smem_optin());
         dim3 grid(p.nchunks, p.tilesA * p.tilesB);
         if (p.stages == 3)
             gram_tcs_kernel<3><<<grid, p.threads, p.smem, st>>>(

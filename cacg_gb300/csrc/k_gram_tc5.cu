@@ -693,12 +693,7 @@ bool gram_tc5_supported(int ka, int kb) {
 
 template <int NC8>
 static void t5_set_attr() {
-    static const bool once = [] {
-        cudaFuncSetAttribute(gram_tc5_kernel<NC8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem_optin());
-        return true;
-    }();
-    (void)once;
+    set_smem_attr(gram_tc5_kernel<NC8>, (int)max_smem_optin());
 }
 
 int launch_gram_reduce(cudaStream_t st, const double *part, int nchunks, int ntiles, int BA,
@@ -707,12 +702,7 @@ int launch_gram_reduce(cudaStream_t st, const double *part, int nchunks, int nti
 
 template <int NC8>
 static void t5m_set_attr() {
-    static const bool once = [] {
-        cudaFuncSetAttribute(gram_tc5m_kernel<NC8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem_optin());
-        return true;
-    }();
-    (void)once;
+    set_smem_attr(gram_tc5m_kernel<NC8>, (int)max_smem_optin());
 }
 
 // The MN-major / TMA kernel; CACG_ERR_UNSUPPORTED when the operands do not

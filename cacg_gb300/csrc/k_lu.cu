@@ -274,12 +274,7 @@ __global__ void __launch_bounds__(32 * kLuWarpsPerCta)
 template <int T>
 static int launch_sweep(cudaStream_t st, int k, const double *F, int r, const double *RHS,
                         double *Y, size_t smem) {
-    static const bool attr = [] {
-        cudaFuncSetAttribute(lu_solve_sweep_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(lu_solve_sweep_kernel<T>, (int)max_smem_optin());
     const int blocks = (r + kLuWarpsPerCta - 1) / kLuWarpsPerCta;
     lu_solve_sweep_kernel<T><<<blocks, 32 * kLuWarpsPerCta, smem, st>>>(k, F, r, RHS, Y);
     return check_launch();
@@ -289,26 +284,14 @@ int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *st
     if (k <= 0) return CACG_ERR_ARG;
     if (k >= kLucCtas && k <= kLucMaxK) {
         const size_t csmem = ((size_t)((k + kLucCtas - 1) / kLucCtas) * k + k) * sizeof(double);
-        static const bool cattr = [] {
-            cudaFuncSetAttribute(lu_factor_cluster_kernel,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(((size_t)(kLucMaxK / kLucCtas) * kLucMaxK + kLucMaxK) *
-                                       sizeof(double)));
-            return true;
-        }();
-        (void)cattr;
+        set_smem_attr(lu_factor_cluster_kernel, (int)(((size_t)(kLucMaxK / kLucCtas) * kLucMaxK + kLucMaxK) * sizeof(double)));
         lu_factor_cluster_kernel<<<kLucCtas, kLucThreads, csmem, st>>>(k, M, F, status);
         if (cudaPeekAtLastError() == cudaSuccess) return check_launch();  // counted
         cudaGetLastError();  // cluster launch refused: the one-CTA factor below
     }
     int use_smem = k <= kLuSmemK;
     size_t smem = use_smem ? (size_t)k * k * sizeof(double) : 0;
-    static const bool attr = [] {
-        cudaFuncSetAttribute(lu_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(lu_factor_kernel, (int)max_smem_optin());
     lu_factor_kernel<<<1, kLuThreads, smem, st>>>(k, M, F, status, use_smem);
     return check_launch();
 }
@@ -333,12 +316,7 @@ int launch_lu_solve(cudaStream_t st, int k, const double *F, int r, const double
     int use_smem = (fbytes + zbytes) <= max_smem_optin() - 1024;
     size_t smem = zbytes + (use_smem ? fbytes : 0);
     if (smem > max_smem_optin()) return CACG_ERR_UNSUPPORTED;
-    static const bool attr = [] {
-        cudaFuncSetAttribute(lu_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(lu_solve_kernel, (int)max_smem_optin());
     int blocks = (r + kLuRC - 1) / kLuRC;
     lu_solve_kernel<<<blocks, kLuRC * kLuTPC, smem, st>>>(k, F, r, RHS, Y, use_smem);
     return check_launch();

@@ -384,12 +384,7 @@ static int launch_rows(cudaStream_t st, int64_t n, const int32_t *rp, const int3
             const size_t max_smem = 96 * 1024;  // keep >= 2 blocks per SM
             while (cap > 16 && (size_t)warps * 2 * cap * (4 + sizeof(T)) > max_smem) cap -= 4;
             const size_t smem = (size_t)warps * 2 * cap * (4 + sizeof(T));
-            static const bool attr = [] {
-                cudaFuncSetAttribute(spmm_ws_kernel<T, CH, TEAM, NCH>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-                return true;
-            }();
-            (void)attr;
+            set_smem_attr(spmm_ws_kernel<T, CH, TEAM, NCH>, 96 * 1024);
             const int64_t nblk = (n + RPW - 1) / RPW;
             dim3 grid(grid_for(nblk, warps), ycols);
             spmm_ws_kernel<T, CH, TEAM, NCH><<<grid, kSpmmThreads, smem, st>>>(

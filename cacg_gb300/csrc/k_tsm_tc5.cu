@@ -880,12 +880,7 @@ int launch_xrupdate_tc5(cudaStream_t st, int64_t n, int k, int m, const float *Q
         return CACG_ERR_UNSUPPORTED;
     if (n == 0) return CACG_OK;
     const size_t smem = tsm_xr_smem(k);
-    static const bool attr = [] {
-        cudaFuncSetAttribute(tsm_xr_tc5_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(tsm_xr_tc5_kernel, (int)max_smem_optin());
     const int64_t ntiles = (n + kTsM - 1) / kTsM;
     const int grid = (int)std::min<int64_t>(ntiles, sm_count());
     tsm_xr_tc5_kernel<<<grid, kTsThreads, smem, st>>>(n, k, m, Q, AQ, ldq, alpha, X, R, S0, lds,
@@ -910,12 +905,7 @@ static int launch_tsm_q(cudaStream_t st, int64_t n, float *Qout, int64_t ldo, co
                         int *status) {
     const int k = 16 * NN;
     const size_t smem = tsm_q_smem(k);
-    static const bool attr = [] {
-        cudaFuncSetAttribute(tsm_q_tc5_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(tsm_q_tc5_kernel<NN>, (int)max_smem_optin());
     int tmem_half = 32;
     while (tmem_half < k) tmem_half *= 2;
     const int64_t ntiles = (n + kTsM - 1) / kTsM;
@@ -941,12 +931,7 @@ static int launch_tsm_qw(cudaStream_t st, int64_t n, float *Qout, int64_t ldo, c
         !tma_encode_2d(&mo, Qout, K, (uint64_t)n, (uint64_t)ldo * 4, kTsKT, 32,
                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE))
         return CACG_ERR_UNSUPPORTED;
-    static const bool attr = [] {
-        cudaFuncSetAttribute(tsm_q_tc5w_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)qw_layout(16 * NN).total);
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(tsm_q_tc5w_kernel<NN>, (int)qw_layout(16 * NN).total);
     int tmem_half = 32;
     while (tmem_half < K) tmem_half *= 2;
     const int64_t ntiles = (n + kTsM - 1) / kTsM;

@@ -121,12 +121,7 @@ int launch_qupdate(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ldo, cons
     int threads = (kQuTR / kQuM) * (BC / kQuN);
     threads = (threads + 31) / 32 * 32;
     size_t smem = need(BC);
-    static const bool attr = [] {
-        cudaFuncSetAttribute(qupdate_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(qupdate_kernel<T>, (int)max_smem_optin());
     int64_t tiles = (n + kQuTR - 1) / kQuTR;
     int64_t cap = (int64_t)sm_count() * 4;
     dim3 grid((unsigned)(tiles < cap ? tiles : cap), (k + BC - 1) / BC);
@@ -285,12 +280,7 @@ int launch_xrupdate(cudaStream_t st, int64_t n, int k, int m, const T *Q, const 
     size_t smem = (size_t)k * m * (8 + 4 + 4) + 16 + (size_t)2 * rows * k * sizeof(T) + 32 +
                   (size_t)rows * mp * 8;
     if (smem > max_smem_optin()) return CACG_ERR_UNSUPPORTED;
-    static const bool attr = [] {
-        cudaFuncSetAttribute(xrupdate_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(xrupdate_kernel<T>, (int)max_smem_optin());
     int G = kRedBlocks;
     int64_t tiles = (n + rows - 1) / rows;
     if (tiles < G) G = (int)(tiles > 0 ? tiles : 1);
@@ -413,12 +403,7 @@ int launch_xrupdate_fast(cudaStream_t st, int64_t n, int k, int m, const T *Q, c
     const int kp = k + 16 / (int)sizeof(T);
     size_t smem = ((size_t)k * mp + 2 * (size_t)TR * kp) * sizeof(T) + (size_t)TR * mp * 8 + 16;
     if (smem > max_smem_optin()) return CACG_ERR_UNSUPPORTED;
-    static const bool attr = [] {
-        cudaFuncSetAttribute(xrupdate_fast_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(xrupdate_fast_kernel<T>, (int)max_smem_optin());
     int G2 = kRedBlocks;
     int64_t tiles = (n + TR - 1) / TR;
     if (tiles < G2) G2 = (int)(tiles > 0 ? tiles : 1);
@@ -622,12 +607,7 @@ int launch_qupdate_direct(cudaStream_t st, int64_t n, int k, T *Qout, int64_t ld
     if (threads > 256) threads = G;  // G <= 256 here
     const int groups_per_block = threads / G;
     size_t smem = (size_t)k * k * sizeof(T);
-    static const bool attr = [] {
-        cudaFuncSetAttribute(qupdate_direct_kernel<T>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(qupdate_direct_kernel<T>, (int)max_smem_optin());
     int64_t ngroups = (n + kDqRows - 1) / kDqRows;
     int64_t blocks = (ngroups + groups_per_block - 1) / groups_per_block;
     int64_t cap = (int64_t)sm_count() * 8;
@@ -650,12 +630,7 @@ int launch_xrupdate_direct(cudaStream_t st, int64_t n, int k, int m, const T *Q,
     const int rows_per_block = threads / G;
     size_t smem = (size_t)k * mp * sizeof(T) + 16 + (size_t)rows_per_block * mp * 8;
     if (smem > max_smem_optin()) return CACG_ERR_UNSUPPORTED;
-    static const bool attr = [] {
-        cudaFuncSetAttribute(xrupdate_direct_kernel<T>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(xrupdate_direct_kernel<T>, (int)max_smem_optin());
     int64_t blocks = (n + rows_per_block - 1) / rows_per_block;
     int64_t cap = std::min<int64_t>((int64_t)sm_count() * 8, kXrMaxBlocks);
     if (blocks > cap) blocks = cap;

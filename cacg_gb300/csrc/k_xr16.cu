@@ -436,12 +436,7 @@ int launch_xt(cudaStream_t st, int64_t n, int k, const float *Q, const float *AQ
         !tma_encode_2d(&ma, AQ, (uint64_t)k, (uint64_t)n, (uint64_t)ldq * 4, 32, kXtRows,
                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B))
         return CACG_ERR_UNSUPPORTED;
-    static const bool attr = [] {
-        cudaFuncSetAttribute(xrupdate16_tma_kernel<NBX, FF>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem_optin());
-        return true;
-    }();
-    (void)attr;
+    set_smem_attr(xrupdate16_tma_kernel<NBX, FF>, (int)max_smem_optin());
     const int64_t ntiles = (n + kXtRows - 1) / kXtRows;
     const int grid =
         (int)std::min<int64_t>(ntiles, std::min<int64_t>(sm_count(), kXr16MaxBlocks));

@@ -34,6 +34,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -80,6 +81,16 @@ size_t max_smem_optin() {
         cached[dev] = v > 0 ? (size_t)v : 49152;
     }
     return cached[dev];
+}
+
+void set_smem_attr_fn(const void *fn, int bytes) {
+    static std::mutex mu;
+    static std::set<std::pair<int, const void *>> done;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.insert({dev, fn}).second)
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 // --------------------------------------------------------------- matrices
@@ -282,19 +293,20 @@ double *pinned_scratch(size_t bytes) {
 }
 
 // Keep freed stream-ordered allocations in the device pool (process-local).
+// Set once per device (each device has its own default pool).
 void keep_pool_memory() {
-    static const bool once = [] {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaMemPool_t pool;
-        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-            uint64_t thr = UINT64_MAX;
-            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-        }
-        cudaGetLastError();
-        return true;
-    }();
-    (void)once;
+    static std::atomic<uint64_t> done{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (done.load() & bit) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    cudaGetLastError();
+    done.fetch_or(bit);
 }
 
 // ------------------------------------------------------- phase profiling

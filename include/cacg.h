@@ -256,9 +256,12 @@ int cacg_k_gram(int32_t vtype, int32_t variant, int64_t n, const void *L, int64_
  * latency-critical loop): the split-K scratch is a fixed 16 MiB device array
  * inside libcacg.so, held by every GPU that loads the library until exit.
  * Calls no cudaMalloc/cudaFree.  Shapes whose single-chunk scratch exceeds
- * 16 MiB return CACG_ERR_ARG.  All calls share the array: calls that overlap
- * on the GPU race.  The first call on a device looks up the array's device
- * address; make it before any stream capture. */
+ * 16 MiB return CACG_ERR_ARG.  variant: CACG_GRAM_AUTO, CACG_GRAM_FMA or
+ * CACG_GRAM_DMMA only (others: CACG_ERR_UNSUPPORTED); FP32 inputs take the
+ * FP64-accurate CUDA-core product.  All calls share the array: calls that
+ * overlap on the GPU race.  The first call in each device context (again
+ * after a cudaDeviceReset) looks up the array's device address; make it
+ * before any stream capture. */
 int cacg_k_gram_noalloc(int32_t vtype, int32_t variant, int64_t n, const void *L,
                         int64_t ldl, int32_t ka, const void *R1, int64_t ldr1, int32_t kb1,
                         const void *R2, int64_t ldr2, int32_t kb2, double *C, int32_t ldc,

@@ -66,3 +66,63 @@ def test_noalloc_rejects_oversized_shape(lib, torch_cuda):
     rc = lib.cacg_k_gram_noalloc(F64, 1, 8, ptr(d), 2048, 2048, ptr(d), 2048, 2048, None, 0, 0,
                                  ptr(Cm), 2048, None)
     assert rc == -1
+
+
+@pytest.mark.parametrize("variant", [3, 4, 5, -1, 99])
+def test_noalloc_refuses_other_variants(lib, torch_cuda, variant):
+    """Only the CUDA-core variants (AUTO, FMA, DMMA) run from the fixed array;
+    the tensor-core variants and unknown values are refused, not rerouted."""
+    torch = torch_cuda
+    L = O.gen_rhs("normal", 1000, 16, 1)
+    rc, _ = _gram(lib, torch, lib.cacg_k_gram_noalloc, F64, variant, L, L, L[:, :4])
+    assert rc == -6
+
+
+def _runtime():
+    """The CUDA runtime torch loaded (the default memory pool it reports is the
+    device's, shared with libcacg.so's statically linked runtime)."""
+    import ctypes as C
+
+    for line in open("/proc/self/maps"):
+        if "libcudart.so" in line:
+            return C.CDLL(line.split()[-1])
+    return C.CDLL("libcudart.so")
+
+
+def test_noalloc_allocates_nothing(lib, torch_cuda):
+    """The pool high-water mark stays at zero across the call (the allocating
+    entry point's stream-ordered workspace comes from the same pool), and the
+    device's free memory does not change."""
+    import ctypes as C
+
+    torch = torch_cuda
+    rt = _runtime()
+    L = O.gen_rhs("normal", 100000, 64, 3)
+    R = O.gen_rhs("normal", 100000, 8, 4)
+    dL, dR = dev(torch, L), dev(torch, R)
+    Cm = torch.zeros((64, 72), dtype=torch.float64, device="cuda")
+    args = (F64, 1, 100000, ptr(dL), 64, 64, ptr(dL), 64, 64, ptr(dR), 8, 8, ptr(Cm), 72, None)
+    assert lib.cacg_k_gram(*args) == 0
+    assert lib.cacg_k_gram_noalloc(*args) == 0  # first call: address lookup
+    torch.cuda.synchronize()
+    pool = C.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(C.byref(pool), torch.cuda.current_device()) == 0
+    zero = C.c_uint64(0)
+    USED_HIGH = 8  # cudaMemPoolAttrUsedMemHigh
+    assert rt.cudaMemPoolSetAttribute(pool, USED_HIGH, C.byref(zero)) == 0
+    free0, tot = C.c_size_t(), C.c_size_t()
+    assert rt.cudaMemGetInfo(C.byref(free0), C.byref(tot)) == 0
+    for _ in range(2):
+        assert lib.cacg_k_gram_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    high = C.c_uint64(1)
+    assert rt.cudaMemPoolGetAttribute(pool, USED_HIGH, C.byref(high)) == 0
+    free1 = C.c_size_t()
+    assert rt.cudaMemGetInfo(C.byref(free1), C.byref(tot)) == 0
+    assert high.value == 0
+    assert free1.value == free0.value
+    # and the result is still the allocating entry point's
+    want = torch.zeros_like(Cm)
+    args_w = args[:12] + (ptr(want),) + args[13:]
+    assert lib.cacg_k_gram(*args_w) == 0
+    assert relerr(host(Cm), host(want)) <= 1e-12
