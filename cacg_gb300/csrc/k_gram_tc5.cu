@@ -37,6 +37,8 @@
 
 #include <algorithm>
 
+#include <atomic>
+
 #include "cacg_internal.cuh"
 #include "tc5_util.cuh"
 #include "tma_util.cuh"
@@ -356,7 +358,7 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
     gram_tc5m_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant__ CUtensorMap tmR1,
                      const __grid_constant__ CUtensorMap tmR2, int64_t n, int64_t rows_per_chunk,
                      int ka, int kb1, int kb2, int BA, int tilesB, int tmem_half, int stages,
-                     double *__restrict__ part, int *__restrict__ status) {
+                     double *__restrict__ part, int *__restrict__ status, long long pipe_polls) {
     constexpr int BB = 16 * NC8;
     constexpr int HC = BB / 4;  // accumulator columns per converter thread (a quarter row)
     constexpr unsigned a_bytes = kT5M * kT5KT * 2, b_bytes = BB * kT5KT * 2;
@@ -429,6 +431,7 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
 #pragma unroll
     for (int q = 0; q < HC; ++q) acc_hi[q] = acc_lo[q] = 0.f;
 
+    int64_t issued = 0;  // loader: TMA fills issued
     if (warp < kT5wConvWarps) {
         // ------------------------------------------------------ converters
         int usrc[kT5wUnits], uch[kT5wUnits], udst[kT5wUnits], uslice[kT5wUnits], urow[kT5wUnits];
@@ -503,7 +506,7 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
             const int64_t g = e / kT5Flush;
             const bool ok = __all_sync(0xffffffffu, t5_mbar_wait_or_abort(
                                                         &gdone[g & 1], (unsigned)((g >> 1) & 1),
-                                                        abort_flag));
+                                                        abort_flag, pipe_polls));
             if (!ok) return false;
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             flush(e);
@@ -518,9 +521,10 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
         unsigned qph = 0;
         for (int64_t j = 0; j < nsteps && ok; ++j) {
             const int b = (int)(j % kT5wNB);
-            bool w = t5_mbar_wait_or_abort(&full[q], qph, abort_flag);
+            bool w = t5_mbar_wait_or_abort(&full[q], qph, abort_flag, pipe_polls);
             if (w && j >= kT5wNB)
-                w = t5_mbar_wait_or_abort(&sfree[b], (unsigned)(((j / kT5wNB) - 1) & 1), abort_flag);
+                w = t5_mbar_wait_or_abort(&sfree[b], (unsigned)(((j / kT5wNB) - 1) & 1), abort_flag,
+                                          pipe_polls);
             if (!__all_sync(0xffffffffu, w)) {
                 ok = false;
                 break;
@@ -568,12 +572,11 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
         if (!ok && lane == 0) fail();
     } else if (tid == kT5wConv) {
         // ---------------------------------------------------------- loader
-        int64_t issued = 0;
         int q = 0;
         unsigned qph = 0;  // phase of stage q's current fill
         for (int64_t j = 0; j < nsteps; ++j) {
             if (j > 0 && q == 0) qph ^= 1u;
-            if (j >= stages && !t5_mbar_wait_or_abort(&empty[q], qph ^ 1u, abort_flag)) {
+            if (j >= stages && !t5_mbar_wait_or_abort(&empty[q], qph ^ 1u, abort_flag, pipe_polls)) {
                 fail();
                 break;
             }
@@ -591,9 +594,6 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
             issued = j + 1;
             if (++q == stages) q = 0;
         }
-        if (*abort_flag)  // let the loads in flight land (bounded)
-            for (int64_t j = issued - stages > 0 ? issued - stages : 0; j < issued; ++j)
-                t5_mbar_wait(&full[j % stages], (unsigned)((j / stages) & 1));
     } else if (tid == kT5wConv + 32) {
         // ---------------------------------------------------- MMA issuer
         const unsigned idesc = t5_idesc(kT5M, BB) | (1u << 15) | (1u << 16);  // A, B MN-major
@@ -601,10 +601,11 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
         for (int64_t j = 0; j < nsteps; ++j) {
             const int b = (int)(j % kT5wNB);
             const int64_t g = j / kT5Flush;
-            if (!t5_mbar_wait_or_abort(&sfull[b], (unsigned)((j / kT5wNB) & 1), abort_flag) ||
+            if (!t5_mbar_wait_or_abort(&sfull[b], (unsigned)((j / kT5wNB) & 1), abort_flag,
+                                       pipe_polls) ||
                 (j % kT5Flush == 0 && g >= 2 &&
                  !t5_mbar_wait_or_abort(&gfree[g & 1], (unsigned)(((g >> 1) - 1) & 1),
-                                        abort_flag))) {
+                                        abort_flag, pipe_polls))) {
                 fail();
                 break;
             }
@@ -630,11 +631,22 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
             if (group_end(j)) t5_commit(&gdone[g & 1]);
             last = j;
         }
-        if (*abort_flag && last >= 0)  // the committed MMAs finish before TMEM goes (bounded)
+        // every committed MMA finishes before TMEM goes (bounded), whether or
+        // not another role gave up after this loop ended
+        if (last >= 0) {
             t5_mbar_wait(&sfree[last % kT5wNB], (unsigned)((last / kT5wNB) & 1));
+            const int64_t g = last / kT5Flush;
+            if (group_end(last)) t5_mbar_wait(&gdone[g & 1], (unsigned)((g >> 1) & 1));
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     const int bad = __syncthreads_or(*abort_flag);
+    // after a give-up some fills may never have been consumed: the loader lets
+    // its last `stages` fills land (bounded) before its thread, and so the
+    // CTA and its shared memory, can retire
+    if (bad && tid == kT5wConv)
+        for (int64_t j = issued - stages > 0 ? issued - stages : 0; j < issued; ++j)
+            t5_mbar_wait(&full[j % stages], (unsigned)((j / stages) & 1));
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
@@ -649,6 +661,11 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
     for (int q = 0; q < HC; ++q) out[q] = (double)acc_hi[q] + (double)acc_lo[q];
 }
 
+
+// Poll limit of the warp-specialised Gram's pipeline waits (the drain waits
+// keep kT5SpinLimit): cacg_set_pipeline_wait_limit shortens it so a test can
+// make those waits run out.
+static std::atomic<long long> g_pipe_polls{kT5SpinLimit};
 
 struct T5Plan {
     int BA, BB, tilesA, tilesB, nchunks, tmem_half;
@@ -747,7 +764,8 @@ static int launch_tc5m(cudaStream_t st, const T5Plan &p, int64_t n, const float 
         t5m_set_attr<NC>();                                                                        \
         gram_tc5m_kernel<NC><<<grid, kT5wThreads, smem, st>>>(tmL, tmR1, tmR2, n, p.rows_per_chunk, \
                                                              ka, kb1, kb2, p.BA, p.tilesB,         \
-                                                             p.tmem_half, stages, ws, status);     \
+                                                             p.tmem_half, stages, ws, status,      \
+                                                             g_pipe_polls.load());                 \
         break;
     switch (p.BB / 16) {
         T5M_CASE(1)
@@ -814,3 +832,8 @@ int launch_gram_tc5(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int
 }
 
 }  // namespace cacg
+
+extern "C" int cacg_set_pipeline_wait_limit(int64_t polls) {
+    cacg::g_pipe_polls.store(polls >= 0 ? (long long)polls : cacg::kT5SpinLimit);
+    return CACG_OK;
+}

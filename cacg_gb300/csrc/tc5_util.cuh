@@ -103,10 +103,13 @@ __device__ __forceinline__ bool t5_mbar_wait(uint64_t *bar, unsigned parity) {
     return false;
 }
 
-// bounded wait that also gives up once *abort is set by another warp
+// bounded wait that also gives up once *abort is set by another warp; the
+// pipeline waits of the tcgen05 Gram pass their limit at run time (a test
+// shortens it to exercise the expiry path), every drain wait keeps the full one
 __device__ __forceinline__ bool t5_mbar_wait_or_abort(uint64_t *bar, unsigned parity,
-                                                      const volatile int *abort) {
-    for (long long i = 0; i < kT5SpinLimit; ++i) {
+                                                      const volatile int *abort,
+                                                      long long limit = kT5SpinLimit) {
+    for (long long i = 0; i < limit; ++i) {
         if (t5_mbar_try(bar, parity)) return true;
         if ((i & 63) == 63 && *abort) return false;
     }
