@@ -67,7 +67,8 @@ class DenseType(C.Structure):  # src/DataTypes.h:50-59
 
 class CacgServerConfig(C.Structure):
     _fields_ = [("mem_budget_bytes", C.c_int64), ("max_active", C.c_int32),
-                ("reserved", C.c_int32 * 7)]
+                ("engine", C.c_int32), ("no_graphs", C.c_int32), ("batch_max_rows", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 _lib = None
@@ -111,6 +112,7 @@ _SIGS = {
                                       C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p,
                                       C.c_int64, C.c_int32, C.c_void_p, C.c_int32,
                                       C.c_void_p]),
+    "cacg_set_pipeline_wait_limit": (C.c_int, [C.c_int64]),
     "cacg_k_qupdate": (C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.c_void_p, C.c_int64,
                                  C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "cacg_k_xrupdate": (C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_void_p,
@@ -144,6 +146,9 @@ _SIGS = {
     "cacg_server_wait": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(CacgResult)]),
     "cacg_server_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                     C.POINTER(C.c_int64)]),
+    "cacg_server_engine_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64),
+                                           C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                           C.c_int32]),
     "cacg_server_destroy": (C.c_int, [C.c_void_p]),
     # generators
     "cacg_gen_rows": (C.c_int64, [C.c_int, C.c_int64]),

@@ -47,11 +47,12 @@ def _percentile(x, q):
 
 
 def run(specs, params: S.Params, rate: float | None, mem_budget: int, max_active: int,
-        prefetch: int = 16, poll_interval: float = 2e-4, arrival_seed: int = 12345):
+        prefetch: int = 16, poll_interval: float = 2e-4, arrival_seed: int = 12345,
+        engine: str = "batched", batch_max_rows: int = 0):
     """Drive the server with `specs`.  rate = requests/s of the Poisson
     arrivals, or None for a closed burst (everything arrives at t = 0).
     Returns a dict of latencies (s), throughput and per-request outcomes."""
-    srv = S.Server(mem_budget, max_active)
+    srv = S.Server(mem_budget, max_active, engine=engine, batch_max_rows=batch_max_rows)
     built: queue.Queue = queue.Queue(maxsize=prefetch)
 
     def producer():
@@ -110,6 +111,7 @@ def run(specs, params: S.Params, rate: float | None, mem_budget: int, max_active
     finally:
         submitted_all.set()
         pol.join()
+        engine_stats = srv.engine_stats()
         srv.close()
     if errors:
         raise errors[0]
@@ -118,7 +120,7 @@ def run(specs, params: S.Params, rate: float | None, mem_budget: int, max_active
     infos = [done[i][1] for i in range(K)]
     rhs = sum(sp["m"] for sp in specs)
     return {"latency_s": lat, "makespan_s": end - t0, "requests_per_s": K / (end - t0),
-            "rhs_per_s": rhs / (end - t0), "infos": infos}
+            "rhs_per_s": rhs / (end - t0), "infos": infos, "engine": engine_stats}
 
 
 def summarize(res, specs, tol):

@@ -249,8 +249,15 @@ class Matrix:
 class Server:
     """Continuous-batching solve server (cacg_server_*)."""
 
-    def __init__(self, mem_budget_bytes: int, max_active: int = 4):
-        cfg = L.CacgServerConfig(mem_budget_bytes, max_active)
+    def __init__(self, mem_budget_bytes: int, max_active: int = 4, engine: str = "batched",
+                 graphs: bool = True, batch_max_rows: int = 0):
+        """engine: "batched" (one launch per phase over all admitted requests,
+        steps replayed from CUDA graphs; requests above batch_max_rows rows,
+        0 = 65536, -1 = no limit, take the per-request path) or "streams" (a
+        stream and the single-request solver per request)."""
+        cfg = L.CacgServerConfig(mem_budget_bytes, max_active,
+                                 {"batched": 0, "streams": 1}[engine], 0 if graphs else 1,
+                                 batch_max_rows)
         h = C.c_void_p()
         L.check(L.lib().cacg_server_create(C.byref(cfg), C.byref(h)), "cacg_server_create")
         self.h = h
@@ -289,6 +296,15 @@ class Server:
         q, a, b = C.c_int64(), C.c_int64(), C.c_int64()
         L.lib().cacg_server_stats(self.h, C.byref(q), C.byref(a), C.byref(b))
         return {"queued": q.value, "active": a.value, "bytes_in_use": b.value}
+
+    def engine_stats(self):
+        steps, rep = C.c_int64(), C.c_int64()
+        bps = (C.c_int32 * 8)()
+        L.lib().cacg_server_engine_stats(self.h, C.byref(steps), C.byref(rep), bps, 8)
+        kinds = ["spmm", "gram", "qupdate", "xrupdate"]
+        return {"steps": steps.value, "graph_replays": rep.value,
+                "blocks_per_sm": {"fp64": dict(zip(kinds, bps[:4])),
+                                  "fp32": dict(zip(kinds, bps[4:]))}}
 
     def close(self):
         if self.h:

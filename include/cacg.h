@@ -267,6 +267,15 @@ int cacg_k_gram_noalloc(int32_t vtype, int32_t variant, int64_t n, const void *L
                         const void *R2, int64_t ldr2, int32_t kb2, double *C, int32_t ldc,
                         void *stream);
 
+/* No counterpart in the reference.  Every wait of the tcgen05 kernels on an
+ * mbarrier is bounded; on expiry the kernel drains its own copies and MMAs in
+ * flight, frees its tensor memory, sets a status word and returns, and the
+ * solver reports CACG_ERR_TIMEOUT.  This sets the poll limit of the tcgen05
+ * Gram's pipeline waits (process-wide; polls < 0 restores the default of
+ * 2^22) so that a test can make them run out; the drain waits keep the full
+ * bound. */
+int cacg_set_pipeline_wait_limit(int64_t polls);
+
 /* src/BLAS3.c:794-825 + :579-612 fused: Q = S - Q * beta (in place on Q),
  * Q, S n x k (strides ldq, lds), beta k x k FP64 row-major. */
 int cacg_k_qupdate(int32_t vtype, int64_t n, int32_t k, void *Q, int64_t ldq,
@@ -312,11 +321,27 @@ int64_t cacg_profile_calls(int phase);
 const char *cacg_profile_name(int phase);
 
 /* ----------------------------------------------------------- serving loop */
+/* Serving engines: BATCHED (default) advances every admitted request one
+ * outer iteration per step, each phase one launch over all requests of a
+ * precision class, the step replayed from a CUDA graph; requests beyond its
+ * kernels' limits (s * m > 64, m > 32, s > 16, Lanczos bounds, block CG) and
+ * requests above batch_max_rows rows run on per-request stream workers with
+ * the single-request solver.  STREAMS runs every request that way.
+ * max_active bounds the requests in flight on both paths together. */
+#define CACG_SERVER_BATCHED 0
+#define CACG_SERVER_STREAMS 1
+
 typedef struct cacg_server cacg_server;
 typedef struct cacg_server_config {
     int64_t mem_budget_bytes; /* device bytes admitted requests may hold */
     int32_t max_active;       /* concurrent requests on the device */
-    int32_t reserved[7];
+    int32_t engine;           /* CACG_SERVER_BATCHED (0) or CACG_SERVER_STREAMS */
+    int32_t no_graphs;        /* batched engine: 1 launches each step directly
+                                 instead of replaying its CUDA graph */
+    int32_t batch_max_rows;   /* batched engine: requests with more rows take a
+                                 stream worker and the single-request solver's
+                                 kernels (0: 65536; negative: no limit) */
+    int32_t reserved[4];
 } cacg_server_config;
 
 int cacg_server_create(const cacg_server_config *cfg, cacg_server **out);
@@ -331,6 +356,11 @@ int cacg_server_wait(cacg_server *srv, int64_t ticket, cacg_result *res);
 /* Queue depth, active requests and device bytes in use. */
 int cacg_server_stats(cacg_server *srv, int64_t *queued, int64_t *active,
                       int64_t *bytes_in_use);
+/* Batched engine: steps run, steps replayed from a CUDA graph, and the
+ * autotuned blocks per SM of its kernels (FP64 class: SpMM, Gram, Q update,
+ * X/R update, then the same four for the FP32 class; 0 = not tuned yet). */
+int cacg_server_engine_stats(cacg_server *srv, int64_t *steps, int64_t *graph_replays,
+                             int32_t *blocks_per_sm, int32_t nvals);
 int cacg_server_destroy(cacg_server *srv);
 
 /* ----------------------------------------------------------- input files

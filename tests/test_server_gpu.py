@@ -22,15 +22,16 @@ def _requests():
     return reqs
 
 
-def test_results_identical_alone_and_in_mix(lib):
+@pytest.mark.parametrize("engine", ["batched", "streams"])
+def test_results_identical_alone_and_in_mix(lib, engine):
     reqs = _requests()
     alone = []
-    srv = cg.Server(mem_budget_bytes=2 << 30, max_active=1)
+    srv = cg.Server(mem_budget_bytes=2 << 30, max_active=1, engine=engine)
     for r in reqs:
         t = srv.submit(*r)
         alone.append(srv.wait(t))
     srv.close()
-    srv = cg.Server(mem_budget_bytes=2 << 30, max_active=4)
+    srv = cg.Server(mem_budget_bytes=2 << 30, max_active=4, engine=engine)
     tickets = [srv.submit(*r) for r in reqs]
     mixed = [srv.wait(t) for t in tickets]
     srv.close()
@@ -86,3 +87,80 @@ def test_open_loop_driver_small_stream(lib):
     for lat, info in zip(res["latency_s"], res["infos"]):
         assert lat >= info["seconds"] * 0.99
     assert summ["p99_ms"] >= summ["p50_ms"] > 0
+
+
+def test_batched_fp64_matches_reference(lib):
+    """The batched engine's FP64 requests with the reference's stopping test
+    (||R(:,0)|| < eps, Gerschgorin bounds) against the reference bcbcg_v1 /
+    cbcg_v1 on the same inputs: outer iterations within +-1, solution within
+    1e-6, while sharing every launch with other requests."""
+    specs = [("lap2d", 48, 4, 4), ("lap3d7", 16, 8, 4), ("lap2d", 64, 1, 4), ("lap3d7", 12, 3, 5),
+             ("lap2d", 40, 16, 4)]
+    reqs = []
+    for i, (kind, N, m, s_) in enumerate(specs):
+        rp, ci, v = cg.gen_matrix(kind, N, shift=0.02 * i)
+        B = cg.gen_rhs("normal", len(rp) - 1, m, 200 + i)
+        eps = 1e-8 * float(np.linalg.norm(B[:, 0]))
+        p = cg.Params(s=s_, bounds="gerschgorin", tol=eps, tol_mode="abs_col0", maxit=1000,
+                      precision="fp64")
+        reqs.append((rp, ci, v, B, p))
+    srv = cg.Server(mem_budget_bytes=2 << 30, max_active=8)
+    tickets = [srv.submit(*r) for r in reqs]
+    outs = [srv.wait(t) for t in tickets]
+    st = srv.engine_stats()
+    srv.close()
+    assert st["steps"] > 0 and st["graph_replays"] == st["steps"]
+    for (rp, ci, v, B, p), (X, info) in zip(reqs, outs):
+        if O.ref_available():
+            Xr, itr, _, _ = O.ref_solve(rp, ci, v, B, np.zeros_like(B), p.s, p.tol, None, 1000)
+        else:
+            Xr, itr, _ = O.port_solve(rp, ci, v, B, np.zeros_like(B), p.s, p.tol, None, 1000)
+        assert info["status"] == 0
+        assert abs(info["iterations"] - itr) <= 1, (info["iterations"], itr)
+        assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) <= 1e-6
+
+
+def test_batched_graph_replay_equals_direct_launches(lib):
+    """Replaying the captured step and launching it directly give the same
+    bits (FP64 and mixed requests in one batch)."""
+    reqs = _requests()
+    res = []
+    for graphs in (True, False):
+        srv = cg.Server(mem_budget_bytes=2 << 30, max_active=6, graphs=graphs)
+        tickets = [srv.submit(*r) for r in reqs]
+        res.append([srv.wait(t) for t in tickets])
+        st = srv.engine_stats()
+        srv.close()
+        assert (st["graph_replays"] > 0) == graphs
+    for (Xa, ia), (Xb, ib) in zip(*res):
+        assert np.array_equal(Xa, Xb) and ia["iterations"] == ib["iterations"]
+
+
+def test_autotuner_choices(lib):
+    srv = cg.Server(mem_budget_bytes=1 << 30, max_active=2)
+    r = _requests()[1]  # a mixed request: tunes the FP32 class
+    srv.wait(srv.submit(*r))
+    st = srv.engine_stats()
+    srv.close()
+    assert all(v in (1, 2, 4, 8) for v in st["blocks_per_sm"]["fp32"].values())
+
+
+def test_requests_beyond_batched_limits_run_on_stream_worker(lib):
+    """k = s m > 64, Lanczos bounds and more rows than batch_max_rows leave
+    the batched kernels; such requests still complete, next to batched ones."""
+    rp, ci, v = cg.gen_matrix("lap2d", 40, shift=0.01)
+    B = cg.gen_rhs("normal", 1600, 20, 5)
+    big = cg.Params(s=4, bounds="gerschgorin", tol=1e-8, maxit=500, precision="fp64")  # k = 80
+    lz = cg.Params(s=4, bounds=("lanczos", 30), tol=1e-8, maxit=500, precision="mixed")
+    srv = cg.Server(mem_budget_bytes=2 << 30, max_active=4, batch_max_rows=1000)
+    t1 = srv.submit(rp, ci, v, B, big)
+    t2 = srv.submit(rp, ci, v, B[:, :4].copy(), lz)
+    t3 = srv.submit(*_requests()[0])  # 1600 rows > batch_max_rows
+    t4 = srv.submit(*_requests()[5])  # 1000 rows: batched
+    outs = [srv.wait(t) for t in (t1, t2, t3, t4)]
+    st = srv.engine_stats()
+    srv.close()
+    assert st["steps"] > 0
+    for X, info in outs:
+        assert info["status"] == 0 and info["true_relres_max"] <= 1e-8
+    assert O.port_true_relres(rp, ci, v, B, outs[0][0]).max() <= 1e-8
