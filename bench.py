@@ -376,6 +376,28 @@ def run_gpu_arm(args, w, rank, world):
     bcg_value = m / (g0.elapsed_time(g1) * 1e-3)
     assert infobcg["status"] == 0 and infobcg["true_relres_max"] <= w["tol"]
 
+    # the CSR SpMM (any matrix, e.g. one read from Matrix Market) on the same
+    # workload: one solve per precision with the DIA view switched off, the
+    # basis-step SpMM timed per call against its CSR algorithmic bytes
+    # (values + column indices + row pointers once, block operands once)
+    csr = {}
+    for prec in ("mixed", "fp64"):
+        pc = params(w, prec)
+        pc.spmm_format = "csr"
+        lib.cacg_profile_reset()
+        lib.cacg_profile_enable(1)
+        barrier()
+        ic = solve(pc)
+        barrier()
+        lib.cacg_profile_enable(0)
+        ms_, l_, b_, f_ = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
+        lib.cacg_profile_get(0, C.byref(ms_), C.byref(l_), C.byref(b_), C.byref(f_))
+        calls = max(lib.cacg_profile_calls(0), 1)
+        gbs = b_.value / (ms_.value * 1e-3) / 1e9 if ms_.value > 0 else None
+        csr[prec] = {"per_call_ms": ms_.value / calls, "calls": calls,
+                     "algorithmic_bytes_per_call": b_.value / calls, "gbs": gbs,
+                     "iterations": ic["iterations"], "true_relres_max": ic["true_relres_max"]}
+
     # the workload's second target (tighter tolerance), mixed and FP64, one
     # solve each on the same inputs
     tight = None
@@ -439,6 +461,10 @@ def run_gpu_arm(args, w, rank, world):
                        "true_relres_max": relres},
             "fp64_value": fp64_value, "mixed_vs_fp64": value / world / fp64_value,
             "bcg_fp64_value": bcg_value, "bcg_iterations": infobcg["iterations"],
+            "csr_spmm": {**csr, "hbm_peak_gbs": hbm,
+                         "frac": {k_: (v_["gbs"] or 0) / hbm for k_, v_ in csr.items()},
+                         "bytes": "CSR: nnz (value + 4-byte index) + 4 (n + 1) + block "
+                                  "operands once"},
             "tight_tolerance": tight, "forward_error": fwd,
             "spmm_hbm_gbs": spmm.get("gbs"),
             "spmm_hbm_frac": (spmm.get("gbs") or 0) / hbm,
@@ -458,8 +484,8 @@ def run_gpu_arm(args, w, rank, world):
     return out
 
 
-SERVING = dict(s=4, tol=1e-8, maxit=3000, rr=5, max_active=4, budget_gb=120, seed=4,
-               calib=32)
+SERVING = dict(s=4, tol=1e-8, maxit=3000, rr=5, max_active=32, budget_gb=120, seed=4,
+               calib=200, engine="batched")
 
 
 def run_serving(args):
@@ -478,17 +504,23 @@ def run_serving(args):
     out = {"workload": "2-D 5-pt / 3-D 7-pt Laplacians 50/50, n log-uniform [1e3, 1e6], "
                        "shift U[0, 0.1], 1-16 N(0,1) RHS, seed 4, Poisson arrivals",
            "requests": K, "load": args.serving_load, "max_active": SERVING["max_active"],
+           "engine": SERVING["engine"] + " (requests of at most 65,536 rows batched, larger "
+                     "ones on per-request streams)",
            "mem_budget_gb": SERVING["budget_gb"], "s": SERVING["s"], "tol": SERVING["tol"],
+           "capacity": "closed burst of the first %d requests" % len(calib),
            "latency": "completion - scheduled arrival (queueing, admission, copies, solve)"}
     for prec in ("mixed", "fp64"):
         p = cg.Params(s=SERVING["s"], bounds="gerschgorin", tol=SERVING["tol"],
                       maxit=SERVING["maxit"], precision=prec, rr_period=SERVING["rr"])
-        cal = SV.run(calib, p, None, budget, SERVING["max_active"])
+        cal = SV.run(calib, p, None, budget, SERVING["max_active"], engine=SERVING["engine"])
         rate = args.serving_load * cal["requests_per_s"]
-        res = SV.run(specs, p, rate, budget, SERVING["max_active"])
+        res = SV.run(specs, p, rate, budget, SERVING["max_active"], engine=SERVING["engine"])
         summ = SV.summarize(res, specs, SERVING["tol"])
         summ["capacity_requests_per_s"] = cal["requests_per_s"]
         summ["arrival_rate_per_s"] = rate
+        summ["engine_steps"] = res["engine"]["steps"]
+        summ["engine_graph_replays"] = res["engine"]["graph_replays"]
+        summ["autotuned_blocks_per_sm"] = res["engine"]["blocks_per_sm"]
         out[prec] = summ
     return out
 
@@ -511,6 +543,73 @@ def traffic_for(phase, n):
     return None if t is None else t * n / TRAFFIC_96_N
 
 
+CONFIG4 = dict(kind="varcoef2d", N=1024, m=32, rhs="beta25", seed=3, shift=1e-6, sigma=1.5,
+               lanczos=50, tol=1e-8, maxit=100, rr=5)
+
+
+def run_config4_sweep():
+    """The ill-conditioned configuration at its shape: 2-D variable-coefficient
+    diffusion 1024^2 (log-normal sigma 1.5 edge conductivities, seed 3, +1e-6
+    shift), 32 Beta(2,5) RHS, s = 4 and s = 8 (k = 128 and 256), 50-step
+    Lanczos interval, tol 1e-8, at most 100 outer iterations (the reference's
+    MAXITER, src/bcbcgKernel.c:3), mixed and FP64.  Prints one JSON record."""
+    import ctypes as C
+
+    import torch
+
+    import cacg_gb300 as cg
+
+    c = CONFIG4
+    lib = cg.lib()
+    rp, ci, v = cg.gen_matrix(c["kind"], c["N"], shift=c["shift"], sigma=c["sigma"],
+                              seed=c["seed"])
+    n = len(rp) - 1
+    B = cg.gen_rhs(c["rhs"], n, c["m"], c["seed"])
+    M = cg.Matrix(rp, ci, v, want_fp32=True)
+    dB = torch.from_numpy(B).cuda()
+    dX = torch.zeros_like(dB)
+    out = {"workload": "varcoef2d 1024^2 sigma 1.5 shift 1e-6, 32 Beta(2,5) RHS seed 3, "
+                       "50-step Lanczos interval, tol 1e-8 (all columns, true residual), "
+                       "maxit 100", "n": n, "nnz": len(v), "runs": {}}
+    for s_ in (4, 8):
+        for prec in ("mixed", "fp64"):
+            p = cg.Params(s=s_, bounds=("lanczos", c["lanczos"]), tol=c["tol"], maxit=c["maxit"],
+                          precision=prec, rr_period=c["rr"])
+            dX.zero_()
+            lib.cacg_profile_reset()
+            lib.cacg_profile_enable(1)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            try:
+                info = M.solve_device(dB.data_ptr(), dX.data_ptr(), c["m"], p)
+            except cg.CacgError as e:
+                info = {"error": str(e)}
+            e1.record()
+            torch.cuda.synchronize()
+            lib.cacg_profile_enable(0)
+            ms = e0.elapsed_time(e1)
+            phases = {}
+            for ph in range(8):
+                ms_, l_, b_, f_ = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
+                lib.cacg_profile_get(ph, C.byref(ms_), C.byref(l_), C.byref(b_), C.byref(f_))
+                if l_.value:
+                    phases[lib.cacg_profile_name(ph).decode()] = round(ms_.value, 3)
+            info.pop("true_relres", None)
+            its = info.get("iterations", 0) or 1
+            out["runs"]["%s_s%d" % (prec, s_)] = {
+                "k": s_ * c["m"], "seconds": ms * 1e-3, "ms_per_outer_iteration": ms / its,
+                "converged": info.get("status") == 0,
+                "rhs_per_s": c["m"] / (ms * 1e-3) if info.get("status") == 0 else None,
+                "info": info, "phase_ms": phases}
+            print(json.dumps({"%s_s%d" % (prec, s_): out["runs"]["%s_s%d" % (prec, s_)]}),
+                  file=sys.stderr, flush=True)
+    M.close()
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -519,10 +618,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="st27_128_m16", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serving-requests", type=int, default=300,
+    ap.add_argument("--serving-requests", type=int, default=2000,
                     help="requests of the serving stream per precision (0: skip)")
     ap.add_argument("--serving-load", type=float, default=0.7)
+    ap.add_argument("--sweep", choices=["config4"], default=None,
+                    help="run a recorded sweep instead of the bench line")
     args = ap.parse_args()
+    if args.sweep == "config4":
+        return run_config4_sweep()
     w = WORKLOADS[args.workload]
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
