@@ -328,12 +328,25 @@ __global__ void __launch_bounds__(kBThreads) bk_lu_factor(const BBatch *__restri
 }
 
 // WHICH 0: beta = QtAQ_prev^{-1} QtAS (k columns); WHICH 1: alpha = QtAQ^{-1} QtR
-// (m columns).  One thread per right-hand-side column, the factor and the
-// columns in shared memory: forward substitution through the reciprocals of
-// L's diagonal, back substitution with U's unit diagonal
+// (m columns).  The solves are FP64 work of k^2 FMAs per column, and GB300's
+// FP64 pipe does about two FMAs per clock per SM, so a request's columns are
+// spread over blocks (grid y, kBLuCols columns each).  A block holds the
+// factor and its columns (column-major) in shared memory; a warp sweeps one
+// column: for each row the lanes take strided parts of the dot product with
+// the solved entries and a butterfly of shuffles adds them (a fixed order),
+// then lane 0 finishes the entry -- forward substitution through the
+// reciprocals of L's diagonal, back substitution with U's unit diagonal
 // (src/DLSsolvers.c:156-207).
+constexpr int kBLuCols = 4;
+
+__device__ __forceinline__ double bwarp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 template <int WHICH>
-__global__ void __launch_bounds__(kBMaxK) bk_lu_solve(const BBatch *__restrict__ b) {
+__global__ void __launch_bounds__(32 * kBLuCols) bk_lu_solve(const BBatch *__restrict__ b) {
     extern __shared__ __align__(16) double bl_smem[];
     const int r = blockIdx.x;
     if (r >= b->nr) return;
@@ -341,27 +354,41 @@ __global__ void __launch_bounds__(kBMaxK) bk_lu_solve(const BBatch *__restrict__
     if (!(d.flags & kBActive) || (WHICH == 0 && d.it == 0)) return;
     const int k = d.k, kk = k * k;
     const int nrhs = WHICH == 0 ? k : d.m;
+    const int c0 = blockIdx.y * kBLuCols;
+    if (c0 >= nrhs) return;
+    const int nc = min(kBLuCols, nrhs - c0);
     const double *RHS = WHICH == 0 ? d.QtAS : d.QtR;
     double *Y = WHICH == 0 ? d.beta : d.alpha;
-    double *Fs = bl_smem, *Ys = bl_smem + kk + k;
+    double *Fs = bl_smem, *Yt = bl_smem + kk + k;  // Yt: nc columns of k
     for (int i = threadIdx.x; i < kk + k; i += blockDim.x) Fs[i] = d.F[i];
-    for (int i = threadIdx.x; i < k * nrhs; i += blockDim.x) Ys[i] = RHS[i];
+    for (int i = threadIdx.x; i < k * nc; i += blockDim.x) {
+        const int cl = i / k, row = i - cl * k;
+        Yt[i] = RHS[row * nrhs + c0 + cl];
+    }
     __syncthreads();
-    const int c = threadIdx.x;
-    if (c < nrhs) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp < nc) {
+        double *y = Yt + warp * k;
         for (int i = 0; i < k; ++i) {
-            double v = Ys[i * nrhs + c];
-            for (int jj = 0; jj < i; ++jj) v -= Fs[i * k + jj] * Ys[jj * nrhs + c];
-            Ys[i * nrhs + c] = v * Fs[kk + i];
+            double part = 0.0;
+            for (int jj = lane; jj < i; jj += 32) part = fma(Fs[i * k + jj], y[jj], part);
+            const double dot = bwarp_sum(part);
+            if (lane == 0) y[i] = (y[i] - dot) * Fs[kk + i];
+            __syncwarp();
         }
         for (int i = k - 1; i >= 0; --i) {
-            double v = Ys[i * nrhs + c];
-            for (int jj = i + 1; jj < k; ++jj) v -= Fs[i * k + jj] * Ys[jj * nrhs + c];
-            Ys[i * nrhs + c] = v;
+            double part = 0.0;
+            for (int jj = i + 1 + lane; jj < k; jj += 32) part = fma(Fs[i * k + jj], y[jj], part);
+            const double dot = bwarp_sum(part);
+            if (lane == 0) y[i] = y[i] - dot;
+            __syncwarp();
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < k * nrhs; i += blockDim.x) Y[i] = Ys[i];
+    for (int i = threadIdx.x; i < k * nc; i += blockDim.x) {
+        const int cl = i / k, row = i - cl * k;
+        Y[row * nrhs + c0 + cl] = Yt[i];
+    }
 }
 
 // Q = S - Q_old beta, in place over S (requests past their first iteration).
@@ -527,15 +554,12 @@ int bl_lu_factor(cudaStream_t st, const BBatch *b) {
 }
 
 int bl_lu_solve(cudaStream_t st, const BBatch *b, int which) {
-    const int smem =
-        (int)(sizeof(double) * ((size_t)kBMaxK * kBMaxK + kBMaxK + (size_t)kBMaxK * kBMaxK));
-    if (which == 0) {
-        set_smem_attr(bk_lu_solve<0>, smem);
-        bk_lu_solve<0><<<kBMax, kBMaxK, smem, st>>>(b);
-    } else {
-        set_smem_attr(bk_lu_solve<1>, smem);
-        bk_lu_solve<1><<<kBMax, kBMaxK, smem, st>>>(b);
-    }
+    const int smem = (int)(sizeof(double) * ((size_t)kBMaxK * kBMaxK + kBMaxK + (size_t)kBLuCols * kBMaxK));
+    const dim3 grid(kBMax, kBMaxK / kBLuCols);
+    if (which == 0)
+        bk_lu_solve<0><<<grid, 32 * kBLuCols, smem, st>>>(b);
+    else
+        bk_lu_solve<1><<<grid, 32 * kBLuCols, smem, st>>>(b);
     return check_launch();
 }
 
