@@ -216,20 +216,33 @@ __global__ void __launch_bounds__(kRingThreads + 32, 2)
         int base[kRingBandMax];  // ring row of the block's first row, band b: t BR mod cap
 #pragma unroll
         for (int b = 0; b < kRingBandMax; ++b) base[b] = 0;
+        const int col = col0 + 4 * c;
+        // Z2 (the recurrence's T_{j-1}) from global memory is software-
+        // pipelined one block ahead: block t + 1's rows are requested while
+        // block t waits and computes, so their latency is hidden behind a
+        // whole block instead of the (short) barrier wait
+        float4 z2v[kRingR], z2n[kRingR];
+        auto load_z2 = [&](int tt, float4(&dst)[kRingR]) {
+            const int64_t rb = R0 + (int64_t)tt * kRingBR + rowoff;
+#pragma unroll
+            for (int i = 0; i < kRingR; ++i)
+                dst[i] = Z2 && tt < nbk && rb + i < n
+                             ? *reinterpret_cast<const float4 *>(Z2 + (rb + i) * ldz2 + col)
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+        };
+        load_z2(0, z2v);
         for (int t = 0; t < nbk; ++t, ++u) {
-            // the recurrence operands from global memory do not wait for the
-            // staged rows: their loads go out before the barrier wait
             const int64_t rbase = R0 + (int64_t)t * kRingBR + rowoff;
-            const int col = col0 + 4 * c;
+            load_z2(t + 1, z2n);
+            // Z1 from global memory (when the ring does not hold it) goes out
+            // before the barrier wait
             const bool z1g = Z1 && rd.z1band < 0;
-            float4 z1v[kRingR], z2v[kRingR];
+            float4 z1v[kRingR];
 #pragma unroll
             for (int i = 0; i < kRingR; ++i) {
                 const bool in = rbase + i < n;
                 z1v[i] = z1g && in ? *reinterpret_cast<const float4 *>(Z1 + (rbase + i) * ldz1 + col)
                                    : make_float4(0.f, 0.f, 0.f, 0.f);
-                z2v[i] = Z2 && in ? *reinterpret_cast<const float4 *>(Z2 + (rbase + i) * ldz2 + col)
-                                  : make_float4(0.f, 0.f, 0.f, 0.f);
             }
             const bool ok = __all_sync(0xffffffffu, t5_mbar_wait_or_abort(
                                                         &full[u & 1], (u >> 1) & 1, abort_flag));
@@ -320,6 +333,8 @@ __global__ void __launch_bounds__(kRingThreads + 32, 2)
             // next TMA fill of these slots (proxy fence, then its arrive)
             t5_fence_proxy_async();
             t5_mbar_arrive(&done[u & 1]);
+#pragma unroll
+            for (int i = 0; i < kRingR; ++i) z2v[i] = z2n[i];
         }
     }
 }
