@@ -131,11 +131,14 @@ def make_inputs(w):
     return rp, ci, v, B
 
 
+SPMM_FORMAT = "auto"  # --spmm-format: "csr" runs the headline solves on the CSR kernels
+
+
 def params(w, precision):
     import cacg_gb300 as cg
 
     return cg.Params(s=w["s"], bounds=w["bounds"], tol=w["tol"], maxit=1000,
-                     precision=precision, rr_period=w["rr"])
+                     precision=precision, rr_period=w["rr"], spmm_format=SPMM_FORMAT)
 
 
 # ------------------------------------------------------------ CPU baseline
@@ -621,9 +624,13 @@ def main():
     ap.add_argument("--serving-requests", type=int, default=2000,
                     help="requests of the serving stream per precision (0: skip)")
     ap.add_argument("--serving-load", type=float, default=0.7)
+    ap.add_argument("--spmm-format", choices=["auto", "csr"], default="auto",
+                    help="csr: the headline solves use the CSR SpMM (profiling)")
     ap.add_argument("--sweep", choices=["config4"], default=None,
                     help="run a recorded sweep instead of the bench line")
     args = ap.parse_args()
+    global SPMM_FORMAT
+    SPMM_FORMAT = args.spmm_format
     if args.sweep == "config4":
         return run_config4_sweep()
     w = WORKLOADS[args.workload]
