@@ -184,11 +184,14 @@ int launch_residual_sl(cudaStream_t st, int64_t n, const int32_t *rp, const int3
                        float *S0, int64_t lds, float *R32, double *norms, double *ws,
                        double avg_nnz, Slices S0sl, Slices R32sl);
 
-// Gram: C (ka x (kb1+kb2)) = L^T [R1 | R2] (FP64 accumulation).
+// Gram: C (ka x (kb1+kb2)) = L^T [R1 | R2] (FP64 accumulation).  symmetric:
+// L^T R1 is symmetric (R1 = A L with A symmetric); the FP64 CUDA-core Gram then
+// computes its upper triangle only (one output tile) and mirrors it.
 template <typename T>
 int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl, int ka,
                 const T *R1, int64_t ldr1, int kb1, const T *R2, int64_t ldr2, int kb2,
-                double *C1, int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes);
+                double *C1, int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes,
+                bool symmetric = false);
 size_t gram_workspace_bytes(int64_t n, int ka, int kb);
 
 // Tensor-core Gram of FP32 blocks (three bf16 slices per value, six slice

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kGramMaxThreads)
     gram_fma_kernel(int64_t n, int64_t rows_per_chunk, const T *__restrict__ L, int64_t ldl,
                     int ka, const T *__restrict__ R1, int64_t ldr1, int kb1,
                     const T *__restrict__ R2, int64_t ldr2, int kb2, int BA, int BB,
-                    int tilesB, double *__restrict__ part) {
+                    int tilesB, double *__restrict__ part, int sym) {
     constexpr int KT = GramKT<T>::value;
     using A = typename AccOf<T>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -126,9 +126,36 @@ __global__ void __launch_bounds__(kGramMaxThreads)
     const int tile_a = blockIdx.y / tilesB, tile_b = blockIdx.y % tilesB;
     const int a0 = tile_a * BA, b0 = tile_b * BB;
     const int kb = kb1 + kb2;
-    const int nb = BB / kMB;
-    const int ta = threadIdx.x / nb, tb = threadIdx.x % nb;
-    const bool active = ta < BA / kMA;
+    const int nb = BB / kMB, na = BA / kMA;
+    int ta, tb;
+    bool active;
+    if (!sym) {
+        ta = threadIdx.x / nb;
+        tb = threadIdx.x % nb;
+        active = ta < na;
+    } else {
+        // symmetric leading block (one tile, L^T R1 with R1 = A L): the
+        // threads take its upper-triangular micro-tiles (tb >= ta), then the
+        // micro-tiles of the columns past it; the reduction mirrors the rest
+        const int ntri = na * (na + 1) / 2, nrest = na * (nb - na);
+        int t = threadIdx.x;
+        ta = 0;
+        tb = 0;
+        active = true;
+        if (t < ntri) {
+            while (t >= na - ta) {
+                t -= na - ta;
+                ++ta;
+            }
+            tb = ta + t;
+        } else if (t - ntri < nrest) {
+            t -= ntri;
+            ta = t / (nb - na);
+            tb = na + t % (nb - na);
+        } else {
+            active = false;
+        }
+    }
 
     const int64_t rbeg = (int64_t)blockIdx.x * rows_per_chunk;
     const int64_t rend = min(n, rbeg + rows_per_chunk);
@@ -298,14 +325,17 @@ constexpr int kRedElems = 64;  // output elements per block (x 4 quarters = 256 
 __global__ void __launch_bounds__(4 * kRedElems)
     gram_reduce_kernel(const double *__restrict__ part, int nchunks, int ntiles, int BA, int BB,
                        int tilesB, int ka, int kb, int kb1, double *__restrict__ C1, int ldc1,
-                       double *__restrict__ C2, int ldc2) {
+                       double *__restrict__ C2, int ldc2, int sym) {
     __shared__ double qs[4][kRedElems];
     const int el = threadIdx.x % kRedElems, q = threadIdx.x / kRedElems;
     const int idx = blockIdx.x * kRedElems + el;
     const bool active = idx < ka * kb;
     const int a = active ? idx / kb : 0, b = active ? idx % kb : 0;
-    const int tile = (a / BA) * tilesB + (b / BB);
-    const size_t off = (size_t)tile * BA * BB + (size_t)(a % BA) * BB + (b % BB);
+    // symmetric leading block: the lower triangle reads its mirror image
+    const bool mirror = sym && b < kb1 && a > b;
+    const int pa = mirror ? b : a, pb = mirror ? a : b;
+    const int tile = (pa / BA) * tilesB + (pb / BB);
+    const size_t off = (size_t)tile * BA * BB + (size_t)(pa % BA) * BB + (pb % BB);
     const size_t stride = (size_t)ntiles * BA * BB;
     const int per = (nchunks + 3) / 4;
     const int p0 = q * per, p1 = min(nchunks, p0 + per);
@@ -392,7 +422,8 @@ size_t gram_workspace_bytes(int64_t n, int ka, int kb) {
 template <typename T>
 int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl, int ka,
                 const T *R1, int64_t ldr1, int kb1, const T *R2, int64_t ldr2, int kb2,
-                double *C1, int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes) {
+                double *C1, int ldc1, double *C2, int ldc2, double *ws, size_t ws_bytes,
+                bool symmetric) {
     const int kb = kb1 + kb2;
     if (ka <= 0 || kb <= 0 || n < 0 || !C1 || (kb2 > 0 && !C2)) return CACG_ERR_ARG;
     if (variant != CACG_GRAM_AUTO && variant != CACG_GRAM_FMA && variant != CACG_GRAM_DMMA)
@@ -407,6 +438,13 @@ int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl
     GramPlan p = plan_gram<T>(variant, n, ka, kb);
     size_t need = (size_t)p.nchunks * p.tilesA * p.tilesB * p.BA * p.BB * sizeof(double);
     if (need > ws_bytes || !ws) return CACG_ERR_ARG;
+    // L^T R1 symmetric (R1 = A L, A symmetric): one tile, square leading block
+    const int sym = symmetric && variant == CACG_GRAM_FMA && p.tilesA == 1 && p.tilesB == 1 &&
+                    ka == kb1 && ka % kMA == 0 && p.BA == ka;
+    if (sym) {
+        const int na = p.BA / kMA, nb = p.BB / kMB;
+        p.threads = round_up(na * (na + 1) / 2 + na * (nb - na), 32);
+    }
     dim3 grid(p.nchunks, p.tilesA * p.tilesB);
     if (n > 0) {
         if (variant == CACG_GRAM_DMMA) {
@@ -421,7 +459,8 @@ int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl
             set_smem_attr(gram_fma_kernel<T>, (int)max_smem_optin());
             gram_fma_kernel<T><<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl,
                                                                 ka, R1, ldr1, kb1, R2, ldr2,
-                                                                kb2, p.BA, p.BB, p.tilesB, ws);
+                                                                kb2, p.BA, p.BB, p.tilesB, ws,
+                                                                sym);
         }
         int rc = check_launch();
         if (rc != CACG_OK) return rc;
@@ -432,7 +471,7 @@ int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl
     gram_reduce_kernel<<<(tot + kRedElems - 1) / kRedElems, 4 * kRedElems, 0, st>>>(ws, n > 0 ? p.nchunks : 1,
                                                           p.tilesA * p.tilesB, p.BA, p.BB,
                                                           p.tilesB, ka, kb, kb1, C1, ldc1,
-                                                          C2, ldc2);
+                                                          C2, ldc2, sym && n > 0);
     return check_launch();
 }
 
@@ -441,16 +480,16 @@ int launch_gram_reduce(cudaStream_t st, const double *part, int nchunks, int nti
                        double *C2, int ldc2) {
     int tot = ka * kb;
     gram_reduce_kernel<<<(tot + kRedElems - 1) / kRedElems, 4 * kRedElems, 0, st>>>(
-        part, nchunks, ntiles, BA, BB, tilesB, ka, kb, kb1, C1, ldc1, C2, ldc2);
+        part, nchunks, ntiles, BA, BB, tilesB, ka, kb, kb1, C1, ldc1, C2, ldc2, 0);
     return check_launch();
 }
 
 template int launch_gram<double>(cudaStream_t, int, int64_t, const double *, int64_t, int,
                                  const double *, int64_t, int, const double *, int64_t, int,
-                                 double *, int, double *, int, double *, size_t);
+                                 double *, int, double *, int, double *, size_t, bool);
 template int launch_gram<float>(cudaStream_t, int, int64_t, const float *, int64_t, int,
                                 const float *, int64_t, int, const float *, int64_t, int,
-                                double *, int, double *, int, double *, size_t);
+                                double *, int, double *, int, double *, size_t, bool);
 
 }  // namespace cacg
 
@@ -696,7 +735,7 @@ static int gram_fixed_scratch(cudaStream_t st, int variant, int64_t n, const T *
             set_smem_attr(gram_fma_kernel<T>, (int)max_smem_optin());
             gram_fma_kernel<T><<<grid, p.threads, p.smem, st>>>(n, p.rows_per_chunk, L, ldl,
                                                                 ka, R1, ldr1, kb1, R2, ldr2,
-                                                                kb2, p.BA, p.BB, p.tilesB, ws);
+                                                                kb2, p.BA, p.BB, p.tilesB, ws, 0);
         }
         int rc = check_launch();
         if (rc != CACG_OK) return rc;
@@ -707,7 +746,7 @@ static int gram_fixed_scratch(cudaStream_t st, int variant, int64_t n, const T *
     gram_reduce_kernel<<<(tot + kRedElems - 1) / kRedElems, 4 * kRedElems, 0, st>>>(ws, n > 0 ? p.nchunks : 1,
                                                           p.tilesA * p.tilesB, p.BA, p.BB,
                                                           p.tilesB, ka, kb, kb1, C1, ldc1,
-                                                          C2, ldc2);
+                                                          C2, ldc2, 0);
     return check_launch();
 }
 

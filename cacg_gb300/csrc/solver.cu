@@ -807,7 +807,7 @@ struct Solver {
             rc = launch_gram_tcs(st, n, b.Qsl, k, k, b.AQsl, k, k, b.R32sl, m, m, b.QtAQ, k,
                                  b.QtR, m, b.gram_ws, b.gram_ws_bytes);
         else
-            rc = gram<T>(Q, k, AQ, k, k, Rp, m, m, b.QtAQ, k, b.QtR, m);
+            rc = gram<T>(Q, k, AQ, k, k, Rp, m, m, b.QtAQ, k, b.QtR, m, true);
         prof.end();
         if (rc) return rc;
         prof.begin(CACG_PHASE_LU, 16.0 * k * k, (2.0 / 3.0) * k * k * k + 2.0 * k * k * m);
@@ -835,8 +835,10 @@ struct Solver {
     // Gram with the variant for this precision: the mixed mode uses the
     // tensor-core kernel unless a CUDA-core variant is requested.
     template <typename T>
+    // symmetric: L^T R1 with R1 = A L (Q^T A Q), only its upper triangle is
+    // computed and mirrored (FP64 CUDA-core Gram)
     int gram(const T *Lm, int ka, const T *R1, int64_t ldr1, int kb1, const T *R2, int64_t ldr2,
-             int kb2, double *C1, int ldc1, double *C2, int ldc2) {
+             int kb2, double *C1, int ldc1, double *C2, int ldc2, bool symmetric = false) {
         const int64_t n = A->n;
         if constexpr (std::is_same<T, float>::value) {
             if ((p.gram_variant == CACG_GRAM_AUTO || p.gram_variant == CACG_GRAM_TC5) &&
@@ -850,7 +852,8 @@ struct Solver {
         }
         int v = p.gram_variant == CACG_GRAM_TC ? CACG_GRAM_FMA : p.gram_variant;
         return launch_gram<T>(st, v, n, Lm, k, ka, R1, ldr1, kb1, R2, ldr2, kb2, C1, ldc1, C2,
-                              ldc2, b.gram_ws, b.gram_ws_bytes);
+                              ldc2, b.gram_ws, b.gram_ws_bytes,
+                              symmetric && std::is_same<T, double>::value);
     }
 
     template <typename T>
