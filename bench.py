@@ -428,18 +428,29 @@ def run_gpu_arm(args, w, rank, world):
             tight[prec + "_status"] = it_["status"]
 
     # end to end through the C ABI with host buffers (cacg_solve): A, B and
-    # the initial X go host->device, X comes back, every step
-    # the caller's X (in/out, as cbcg_v1's X) is reset to x0 = 0 every step
-    Xh = np.zeros_like(B)
+    # the initial X go host->device, X comes back, every step; the caller's
+    # arrays sit in pinned host memory (torch's pinned allocator, viewed as
+    # numpy), and the caller's X (in/out, as cbcg_v1's X) is reset to x0 = 0
+    # every step
+    def pinned(a):
+        t = torch.empty(a.shape, dtype={np.int32: torch.int32, np.float64: torch.float64}[
+            a.dtype.type], pin_memory=True)
+        out = t.numpy()
+        out[...] = a
+        return out, t
+
+    (rp_h, _t1), (ci_h, _t2), (v_h, _t3), (B_h, _t4) = (pinned(rp), pinned(ci), pinned(v),
+                                                         pinned(B))
+    Xh, _t5 = pinned(np.zeros_like(B))
     hb = 4 * (n + 1) + 12 * nnz + 2 * 8 * n * m
     db = 8 * n * m
-    _X, _ = cg.solve(rp, ci, v, B, Xh, params=pm, overwrite_x0=True)  # warm-up
+    _X, _ = cg.solve(rp_h, ci_h, v_h, B_h, Xh, params=pm, overwrite_x0=True)  # warm-up
     k_e2e = max(1, min(args.steps, 3))
     barrier()
     t0 = time.perf_counter()
     for _ in range(k_e2e):
         Xh.fill(0.0)
-        Xe, ie = cg.solve(rp, ci, v, B, Xh, params=pm, overwrite_x0=True)
+        Xe, ie = cg.solve(rp_h, ci_h, v_h, B_h, Xh, params=pm, overwrite_x0=True)
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / k_e2e
     assert ie["true_relres_max"] <= w["tol"]
@@ -480,7 +491,8 @@ def run_gpu_arm(args, w, rank, world):
                          "algorithmic_bytes_per_call": d["bytes"] / max(d["calls"], 1)},
             "phases": phases,
             "e2e": {"value": m / e2e_s, "unit": "RHS/s", "h2d_bytes_per_step": hb,
-                    "d2h_bytes_per_step": db},
+                    "d2h_bytes_per_step": db, "host_memory": "pinned",
+                    "path": "cacg_solve (matrix upload and DIA view, B and X0 up, X down)"},
             "clocks": clk, "gpu_launches": launches,
         }
     M.close()
