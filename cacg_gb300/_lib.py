@@ -118,6 +118,8 @@ _SIGS = {
     "cacg_k_xrupdate": (C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_void_p,
                                   C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "cacg_k_tsqr": (C.c_int, [C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p,
+                              C.c_int64, C.c_void_p, C.c_void_p]),
     "cacg_k_lu": (C.c_int, [C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                             C.c_void_p, C.c_void_p]),
     # input files

@@ -30,7 +30,7 @@ CU_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 C_FLAGS = ["-O2", "-fPIC", "-std=gnu99", "-ffp-contract=off",
            "-I", os.path.join(REPO, "include")]
 
-CU_SOURCES = ["k_spmm.cu", "k_gram.cu", "k_gram_tc.cu", "k_gram_tc5.cu", "k_tsm_tc5.cu", "k_dia.cu", "k_dia_ring.cu", "k_dia_wide.cu", "k_update.cu", "k_xr16.cu", "k_lu.cu", "solver.cu", "bcg.cu", "server.cu", "k_batch.cu"]
+CU_SOURCES = ["k_spmm.cu", "k_gram.cu", "k_gram_tc.cu", "k_gram_tc5.cu", "k_tsm_tc5.cu", "k_dia.cu", "k_dia_ring.cu", "k_dia_wide.cu", "k_update.cu", "k_xr16.cu", "k_lu.cu", "solver.cu", "bcg.cu", "server.cu", "k_batch.cu", "k_tsqr.cu"]
 C_SOURCES = ["cacg_gen.c", "cacg_io.c"]
 HEADERS = ["cacg_internal.cuh", "cacg_solver.h", "tc5_util.cuh", "ff_util.cuh", "tma_util.cuh",
            "batch.h"]

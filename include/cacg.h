@@ -289,6 +289,16 @@ int cacg_k_xrupdate(int32_t vtype, int64_t n, int32_t k, int32_t m, const void *
                     const void *AQ, int64_t ldq, const double *alpha, double *X,
                     double *R, void *S0, int64_t lds, double *norms, void *stream);
 
+/* Tall-skinny QR, V (n x k, FP64, row-major, stride ldv) = Q R: Q (n x k,
+ * stride ldq) with orthonormal columns, R (k x k row-major) upper triangular
+ * with a positive diagonal; k <= 128, n >= k.  The reference's TSQR
+ * (src/TSQR.c) is empty and its Householder QR (src/MatrixDecomposition.c:3-93)
+ * unfinished, so this has no reference behaviour to match: CholeskyQR2 on the
+ * split-K FP64 Gram, orthogonal to working accuracy for cond(V) < ~1e8;
+ * CACG_ERR_BREAKDOWN when V is numerically rank-deficient. */
+int cacg_k_tsqr(int64_t n, int32_t k, const double *V, int64_t ldv, double *Q, int64_t ldq,
+                double *R, void *stream);
+
 /* src/DLSsolvers.c:106-208 LUsolver_v1_KeeplhsMat: Y (k x r) = M^{-1} RHS by
  * Crout LU without pivoting (U unit-diagonal).  status (device int, may be
  * NULL) is set to 1 on a zero or non-finite pivot. */
