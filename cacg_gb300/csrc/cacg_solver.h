@@ -97,6 +97,9 @@ size_t solve_workspace_bytes(int64_t n, int m, int s, int prec, bool lanczos);
 // Solve with device B, X.  ws_external (>= solve_workspace_bytes) may be
 // given; otherwise a cached workspace is used.
 void keep_pool_memory();
+// phase profiler (cacg_profile_*): on/off, and a call timed by another component
+bool profile_enabled();
+void profile_accumulate(int phase, double ms, int64_t launches);
 
 int solve_on_device(const DevMatrix *A, const double *B, double *X, int m,
                     const cacg_params *p, cacg_result *res, void *ws_external,

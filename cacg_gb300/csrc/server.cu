@@ -285,6 +285,11 @@ struct Engine {
     std::map<std::tuple<int, int>, G> gcache;  // (longest basis FP64, FP32; 0 = class absent)
 
     ~Engine() {
+        for (auto &pm : marks) {
+            cudaEventDestroy(pm.a);
+            cudaEventDestroy(pm.b);
+        }
+        for (auto e : event_pool) cudaEventDestroy(e);
         for (auto &kv : gcache)
             if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
         for (int c = 0; c < 2; ++c)
@@ -358,21 +363,63 @@ struct Engine {
         return v;
     }
 
+    // phase timing of direct (not graph-replayed) steps while the profiler is
+    // on: events around each phase, read after the step's synchronisation
+    struct PhaseMark {
+        int phase;
+        cudaEvent_t a, b;
+    };
+    std::vector<PhaseMark> marks;
+    std::vector<cudaEvent_t> event_pool;
+    bool timing = false;
+    cudaEvent_t ev() {
+        if (!event_pool.empty()) {
+            cudaEvent_t e = event_pool.back();
+            event_pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+    template <class F>
+    int timed(int phase, F &&f) {
+        if (!timing) return f();
+        PhaseMark pm{phase, ev(), ev()};
+        cudaEventRecord(pm.a, st);
+        const int rc = f();
+        cudaEventRecord(pm.b, st);
+        marks.push_back(pm);
+        return rc;
+    }
+    void harvest_marks() {
+        for (auto &pm : marks) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, pm.a, pm.b) == cudaSuccess)
+                profile_accumulate(pm.phase, ms, 0);
+            cudaGetLastError();
+            event_pool.push_back(pm.a);
+            event_pool.push_back(pm.b);
+        }
+        marks.clear();
+    }
+
     // one outer iteration of every slot of class `cls` (T: its precision)
     template <typename T>
     int iteration_launches(int cls, int sm) {
         const BBatch *b = d_b[cls];
         const BTune &tu = tune[cls];
         int rc = CACG_OK;
-        for (int j = 1; j < sm && rc == CACG_OK; ++j) rc = bl_basis_step<T>(st, b, j, tu);
-        if (rc == CACG_OK) rc = bl_gram<T>(st, b, 0, tu);
-        if (rc == CACG_OK) rc = bl_lu_solve(st, b, 0);
-        if (rc == CACG_OK) rc = bl_qupdate<T>(st, b, tu);
-        if (rc == CACG_OK) rc = bl_aq<T>(st, b, tu);
-        if (rc == CACG_OK) rc = bl_gram<T>(st, b, 1, tu);
-        if (rc == CACG_OK) rc = bl_lu_factor(st, b);
-        if (rc == CACG_OK) rc = bl_lu_solve(st, b, 1);
-        if (rc == CACG_OK) rc = bl_xrupdate<T>(st, b, tu);
+        for (int j = 1; j < sm && rc == CACG_OK; ++j)
+            rc = timed(CACG_PHASE_BASIS, [&] { return bl_basis_step<T>(st, b, j, tu); });
+        if (rc == CACG_OK) rc = timed(CACG_PHASE_GRAM, [&] { return bl_gram<T>(st, b, 0, tu); });
+        if (rc == CACG_OK) rc = timed(CACG_PHASE_LU, [&] { return bl_lu_solve(st, b, 0); });
+        if (rc == CACG_OK) rc = timed(CACG_PHASE_QUPDATE, [&] { return bl_qupdate<T>(st, b, tu); });
+        if (rc == CACG_OK) rc = timed(CACG_PHASE_AQ, [&] { return bl_aq<T>(st, b, tu); });
+        if (rc == CACG_OK) rc = timed(CACG_PHASE_GRAM, [&] { return bl_gram<T>(st, b, 1, tu); });
+        if (rc == CACG_OK) rc = timed(CACG_PHASE_LU, [&] { return bl_lu_factor(st, b); });
+        if (rc == CACG_OK) rc = timed(CACG_PHASE_LU, [&] { return bl_lu_solve(st, b, 1); });
+        if (rc == CACG_OK) rc = timed(CACG_PHASE_XRUPDATE, [&] { return bl_xrupdate<T>(st, b, tu); });
         return rc;
     }
 
@@ -431,10 +478,13 @@ struct Engine {
             srv->engine_graph_replays++;
             rc = CACG_OK;
         } else {
+            timing = profile_enabled();
             rc = step_launches(sm0, sm1);
+            timing = false;
         }
         if (rc != CACG_OK) return rc;
         if (cudaStreamSynchronize(st) != cudaSuccess) return CACG_ERR_CUDA;
+        harvest_marks();
         srv->engine_steps++;
         return CACG_OK;
     }
@@ -453,8 +503,12 @@ struct Engine {
             if (cudaMemcpyAsync(d_b[c], h_b[c], sizeof(BBatch), cudaMemcpyHostToDevice, st) !=
                 cudaSuccess)
                 return CACG_ERR_CUDA;
-            const int rc = c == 0 ? bl_residual<double>(st, d_b[c], tune[c])
-                                  : bl_residual<float>(st, d_b[c], tune[c]);
+            timing = profile_enabled();
+            const int rc = timed(CACG_PHASE_RESIDUAL, [&] {
+                return c == 0 ? bl_residual<double>(st, d_b[c], tune[c])
+                              : bl_residual<float>(st, d_b[c], tune[c]);
+            });
+            timing = false;
             if (rc) return rc;
         }
         if (!any) return CACG_OK;
@@ -462,6 +516,7 @@ struct Engine {
                             cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess)
             return CACG_ERR_CUDA;
+        harvest_marks();
         return CACG_OK;
     }
 

@@ -319,6 +319,17 @@ struct PhaseAcc {
 };
 static PhaseAcc g_prof[CACG_NUM_PHASES];
 
+bool profile_enabled() { return g_prof_on.load() != 0; }
+
+// a timed call of `phase` measured outside the solver (the serving engine)
+void profile_accumulate(int phase, double ms, int64_t launches) {
+    if (phase < 0 || phase >= CACG_NUM_PHASES) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof[phase].ms += ms;
+    g_prof[phase].launches += launches;
+    g_prof[phase].calls += 1;
+}
+
 struct PendingEv {
     cudaEvent_t a, b;
     int phase;
