@@ -3,10 +3,10 @@
 // The engine advances every admitted request by one outer iteration per
 // step; each phase of the iteration is ONE launch over all requests of a
 // precision class.  A launch walks a tile table: request r owns the tiles
-// [tile_start[r], tile_start[r+1]) (row tiles of kBRows rows, or Gram chunks
-// of bchunk rows); blocks stride over the table, so the grid size is free
+// [tile_start[r], tile_start[r+1]) (row tiles of kBRows rows, or Gram pieces
+// of bpiece rows); blocks stride over the table, so the grid size is free
 // (the autotuner picks it) and never changes a result.  Every reduction is
-// partitioned by the request's own shape only (row tiles, Gram chunks, fixed
+// partitioned by the request's own shape only (row tiles, Gram pieces, fixed
 // summation order), so a request's iterates are bit-identical whether it ran
 // alone or with others.
 #pragma once
@@ -23,13 +23,19 @@ constexpr int kBMaxS = 16;      // basis length s
 constexpr int kBRows = 128;     // rows per row tile (SpMM, updates, norms)
 constexpr int kBThreads = 256;
 
-// rows per Gram chunk (split-K): both operands' rows of a chunk fit in
-// shared memory (80 KB at the largest shapes)
+// Gram split-K: a block takes one piece of a request (bpiece rows), staged
+// through shared memory bgchunk rows at a time; the piece's sums stay in
+// registers (FP32 class: FP32 over the piece's 256 rows, the single-request
+// tensor-core Gram's group length) and are written as one FP64 partial.
 template <typename T>
-__host__ __device__ constexpr int bchunk() {
-    return sizeof(T) == 4 ? 128 : 64;
+__host__ __device__ constexpr int bgchunk() {
+    return sizeof(T) == 4 ? 64 : 32;
 }
-inline int bchunk_rows(bool f32) { return f32 ? 128 : 64; }
+template <typename T>
+__host__ __device__ constexpr int bpiece() {
+    return 4 * bgchunk<T>();
+}
+inline int bpiece_rows(bool f32) { return f32 ? bpiece<float>() : bpiece<double>(); }
 
 // request flags
 constexpr int kBActive = 1;     // takes part in this step's iteration
@@ -45,22 +51,23 @@ struct BDesc {
     void *S;            // basis of this step; Q after the update
     void *Qold;         // Q of the previous step; receives the next T_0
     void *AQ;
-    double *QtAS, *QtAQ, *QtR, *F, *alpha, *beta;
+    double *QtAS, *QtAQ, *QtR, *alpha, *beta;
+    double *F;          // LU: the factors (k x k), 1 / L_ii (k), the factors transposed (k x k)
     double *norms;      // m: squared column norms (recurrence or residual)
-    double *gpart;      // Gram partials: nchunk x k x (k + m)
+    double *gpart;      // Gram partials: npiece x k x (k + m)
     double *npart;      // norm partials: ntile x m
     int *status;
     int64_t n;
     int m, s, k, it;
-    int flags, ntile, nchunk, pad;
+    int flags, ntile, npiece, pad;
     double sa, sb;      // Chebyshev map: 2 / (lmax - lmin), -(lmax + lmin) / (lmax - lmin)
 };
 
 struct BBatch {
     int nr;
-    int total_tiles, total_chunks, pad;
+    int total_tiles, total_pieces, pad;
     int tile_start[kBMax + 1];
-    int chunk_start[kBMax + 1];
+    int piece_start[kBMax + 1];
     BDesc d[kBMax];
 };
 

@@ -90,8 +90,8 @@ struct BLayout {
 static BLayout blayout(int64_t n, int64_t nnz, int m, int s, bool f32) {
     const int k = s * m;
     const size_t es = f32 ? 4 : 8;
-    const int ch = bchunk_rows(f32);
-    const int64_t ntile = (n + kBRows - 1) / kBRows, nchunk = (n + ch - 1) / ch;
+    const int pr = bpiece_rows(f32);
+    const int64_t ntile = (n + kBRows - 1) / kBRows, npiece = (n + pr - 1) / pr;
     BLayout L{};
     size_t o = 0;
     auto put = [&](size_t &field, size_t bytes) {
@@ -109,9 +109,9 @@ static BLayout blayout(int64_t n, int64_t nnz, int m, int s, bool f32) {
     put(L.S, (size_t)n * k * es);
     put(L.Q, (size_t)n * k * es);
     put(L.AQ, (size_t)n * k * es);
-    // QtAS, QtAQ, beta k x k; F k x k + k; QtR, alpha k x m; bounds 2
-    put(L.small, sizeof(double) * ((size_t)4 * k * k + k + (size_t)2 * k * m + 2));
-    put(L.gpart, sizeof(double) * (size_t)nchunk * k * (k + m));
+    // QtAS, QtAQ, beta k x k; F 2 k x k + k; QtR, alpha k x m; bounds 2
+    put(L.small, sizeof(double) * ((size_t)5 * k * k + k + (size_t)2 * k * m + 2));
+    put(L.gpart, sizeof(double) * (size_t)npiece * k * (k + m));
     put(L.npart, sizeof(double) * (size_t)ntile * m);
     put(L.gws, sizeof(double) * 2 * 320);  // Gerschgorin partials
     L.total = o;
@@ -338,22 +338,22 @@ struct Engine {
         BBatch *b = h_b[cls];
         const int nr = (int)slots[cls].size();
         b->nr = nr;
-        int tiles = 0, chunks = 0;
+        int tiles = 0, pieces = 0;
         for (int i = 0; i < nr; ++i) {
             BSlot &s = *slots[cls][i];
             b->tile_start[i] = tiles;
-            b->chunk_start[i] = chunks;
+            b->piece_start[i] = pieces;
             tiles += s.d.ntile;
-            chunks += s.d.nchunk;
+            pieces += s.d.npiece;
             b->d[i] = s.d;
             b->d[i].norms = norms_of(cls, i);
             b->d[i].status = d_status + cls * kBMax + i;
             b->d[i].flags = flag_of(s);
         }
         b->tile_start[nr] = tiles;
-        b->chunk_start[nr] = chunks;
+        b->piece_start[nr] = pieces;
         b->total_tiles = tiles;
-        b->total_chunks = chunks;
+        b->total_pieces = pieces;
         return nr;
     }
 
@@ -550,7 +550,7 @@ struct Engine {
         d.QtAS = sm; sm += (size_t)k * k;
         d.QtAQ = sm; sm += (size_t)k * k;
         d.beta = sm; sm += (size_t)k * k;
-        d.F = sm; sm += (size_t)k * k + k;
+        d.F = sm; sm += (size_t)2 * k * k + k;
         d.QtR = sm; sm += (size_t)k * m;
         d.alpha = sm; sm += (size_t)k * m;
         s.bounds = sm;
@@ -563,7 +563,7 @@ struct Engine {
         d.k = k;
         d.it = 0;
         d.ntile = (int)((r->n + kBRows - 1) / kBRows);
-        d.nchunk = (int)((r->n + bchunk_rows(f32) - 1) / bchunk_rows(f32));
+        d.npiece = (int)((r->n + bpiece_rows(f32) - 1) / bpiece_rows(f32));
         const size_t bx = (size_t)r->n * m * 8;
         if (cudaMemcpyAsync((void *)d.rp, r->rp.data(), (size_t)(r->n + 1) * 4,
                             cudaMemcpyHostToDevice, st) != cudaSuccess ||
