@@ -120,6 +120,44 @@ def test_batched_fp64_matches_reference(lib):
         assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) <= 1e-6
 
 
+def test_batched_edge_shapes(lib):
+    """Shapes at the batched kernels' edges, all in one batch: one partial row
+    tile (n = 81), k not a multiple of 4 (21, 25, 51), m = 1 and m = 32, k = 64
+    (at m = 32 the Gram's tile count exceeds the block and takes two passes),
+    and a request of many Gram pieces (n = 40,000).  FP64 requests against the
+    oracle's bcbcg (outer iterations within +-1, solution within 1e-6); mixed
+    requests reach the tolerance on the true residual."""
+    specs = [("lap2d", 9, 1, 2), ("lap3d7", 10, 32, 2), ("lap2d", 30, 8, 8), ("lap2d", 37, 7, 3),
+             ("lap3d7", 13, 5, 5), ("lap2d", 200, 3, 4), ("lap3d7", 11, 17, 3)]
+    reqs = []
+    for i, (kind, N, m, s_) in enumerate(specs):
+        rp, ci, v = cg.gen_matrix(kind, N, shift=0.05 + 0.01 * i)
+        B = cg.gen_rhs("normal", len(rp) - 1, m, 300 + i)
+        eps = 1e-8 * float(np.linalg.norm(B[:, 0]))
+        p64 = cg.Params(s=s_, bounds="gerschgorin", tol=eps, tol_mode="abs_col0", maxit=1000,
+                        precision="fp64")
+        pmx = cg.Params(s=s_, bounds="gerschgorin", tol=1e-8, maxit=1000, precision="mixed")
+        reqs.append((rp, ci, v, B, p64))
+        reqs.append((rp, ci, v, B, pmx))
+    srv = cg.Server(mem_budget_bytes=4 << 30, max_active=16)
+    tickets = [srv.submit(*r) for r in reqs]
+    outs = [srv.wait(t) for t in tickets]
+    st = srv.engine_stats()
+    srv.close()
+    assert st["steps"] > 0
+    for (rp, ci, v, B, p), (X, info) in zip(reqs, outs):
+        assert info["status"] == 0, (len(rp) - 1, B.shape, p.s, p.precision)
+        if p.precision == "fp64":
+            if O.ref_available():
+                Xr, itr, _, _ = O.ref_solve(rp, ci, v, B, np.zeros_like(B), p.s, p.tol, None, 1000)
+            else:
+                Xr, itr, _ = O.port_solve(rp, ci, v, B, np.zeros_like(B), p.s, p.tol, None, 1000)
+            assert abs(info["iterations"] - itr) <= 1, (info["iterations"], itr)
+            assert np.linalg.norm(X - Xr) / np.linalg.norm(Xr) <= 1e-6
+        else:
+            assert O.port_true_relres(rp, ci, v, B, X).max() <= 1e-8
+
+
 def test_batched_graph_replay_equals_direct_launches(lib):
     """Replaying the captured step and launching it directly give the same
     bits (FP64 and mixed requests in one batch)."""
