@@ -256,12 +256,24 @@ __global__ void __launch_bounds__(kBThreads) bk_spmm(const BBatch *__restrict__ 
         const int p0 = sh.rps[0];
         const int ng = (w + 3) >> 2;
         const uint32_t mg = bdiv_magic(ng);
+        // a row's 4-column piece of Q is 16-byte aligned (FP64: 32 bytes, two loads)
+        const bool vec = ((uintptr_t)X & 15) == 0 && (k & 3) == 0;
         for (int e = threadIdx.x; e < rows * ng; e += kBThreads) {
             const int lr = bdiv(e, ng, mg), c0 = 4 * (e - lr * ng), nc = min(4, w - c0);
             const int64_t row = row0 + lr;
             const int q0 = sh.rps[lr] - p0, q1 = sh.rps[lr + 1] - p0;
             T acc[4] = {(T)0.0, (T)0.0, (T)0.0, (T)0.0};
-            if (staged) {
+            if (MODE == 1 && staged && vec && nc == 4) {
+                // A Q: 16-byte gathers of the 4 columns (same FMAs, same order)
+#pragma unroll 4
+                for (int q = q0; q < q1; ++q) {
+                    const T v = sh.vs[q];
+                    T xv[4];
+                    ld4(X + (int64_t)sh.cis[q] * k + c0, xv);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) acc[u] = fma(v, xv[u], acc[u]);
+                }
+            } else if (staged) {
 #pragma unroll 2
                 for (int q = q0; q < q1; ++q) {
                     const T v = sh.vs[q];

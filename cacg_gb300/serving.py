@@ -48,19 +48,23 @@ def _percentile(x, q):
 
 def run(specs, params: S.Params, rate: float | None, mem_budget: int, max_active: int,
         prefetch: int = 16, poll_interval: float = 2e-4, arrival_seed: int = 12345,
-        engine: str = "batched", batch_max_rows: int = 0):
+        engine: str = "batched", batch_max_rows: int = 0, prebuild: bool = False):
     """Drive the server with `specs`.  rate = requests/s of the Poisson
     arrivals, or None for a closed burst (everything arrives at t = 0).
+    prebuild: every request is built before the clock starts (otherwise a
+    producer thread builds them at most `prefetch` ahead of submission).
     Returns a dict of latencies (s), throughput and per-request outcomes."""
     srv = S.Server(mem_budget, max_active, engine=engine, batch_max_rows=batch_max_rows)
-    built: queue.Queue = queue.Queue(maxsize=prefetch)
+    built: queue.Queue = queue.Queue(maxsize=len(specs) if prebuild else prefetch)
 
     def producer():
         for sp in specs:
             built.put(build_request(sp))
 
-    prod = threading.Thread(target=producer, daemon=True)
-    prod.start()
+    if prebuild:
+        producer()
+    else:
+        threading.Thread(target=producer, daemon=True).start()
     K = len(specs)
     if rate:
         gaps = np.random.default_rng(arrival_seed).exponential(1.0 / rate, K)
@@ -133,3 +137,38 @@ def summarize(res, specs, tol):
             "requests_per_s": res["requests_per_s"],
             "all_converged": all(s == 0 for s in st) and max(rr) <= tol,
             "true_relres_max": float(max(rr))}
+
+
+def main(argv=None):
+    """Command line: one run of the serving stream's first `--requests`
+    requests (a closed burst, or Poisson arrivals at `--rate` requests/s),
+    printing the latency summary and the engine's counters as one JSON line.
+    Example: python -m cacg_gb300.serving --requests 64 --max-rows 65536 --prebuild"""
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(prog="python -m cacg_gb300.serving")
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--engine", choices=["batched", "streams"], default="batched")
+    ap.add_argument("--rate", type=float, default=None, help="requests/s (default: closed burst)")
+    ap.add_argument("--max-active", type=int, default=32)
+    ap.add_argument("--max-rows", type=float, default=1e6,
+                    help="largest request size of the stream (n log-uniform in [1e3, this])")
+    ap.add_argument("--budget-gb", type=int, default=120)
+    ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--prebuild", action="store_true",
+                    help="build every request before the clock starts")
+    a = ap.parse_args(argv)
+    specs = request_specs(a.requests, seed=a.seed, nmax=a.max_rows)
+    p = S.Params(s=4, bounds="gerschgorin", tol=1e-8, maxit=3000, precision=a.precision,
+                 rr_period=5)
+    res = run(specs, p, a.rate, a.budget_gb << 30, a.max_active, engine=a.engine,
+              prebuild=a.prebuild)
+    out = summarize(res, specs, 1e-8)
+    out.update(engine=a.engine, precision=a.precision, engine_stats=res["engine"])
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()
