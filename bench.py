@@ -562,6 +562,50 @@ CONFIG4 = dict(kind="varcoef2d", N=1024, m=32, rhs="beta25", seed=3, shift=1e-6,
                lanczos=50, tol=1e-8, maxit=100, rr=5)
 
 
+def run_gram64_sweep():
+    """The FP64 Gram Q^T [A Q | R] of the FP64 mode at k = 96 (s = 6, m = 16)
+    on both FP64 kernels: the split-K FMA kernel (the FP64 mode's choice) and
+    the split-K FP64 tensor-core kernel (mma.sync m8n8k4 f64), n = 294,912
+    rows of N(0, 1) FP64 operands (0.49 GB, above L2), five calls each after a
+    warm-up, CUDA events.  Prints one JSON record: ms per call, TFLOP/s
+    (2 n k (k + m) flops) and the largest difference between the two
+    results relative to the largest entry."""
+    import torch
+
+    import cacg_gb300 as cg
+
+    lib = cg.lib()
+    n, k, m = 294912, 96, 16
+    g = torch.Generator(device="cuda").manual_seed(1)
+    L = torch.randn(n, k, dtype=torch.float64, device="cuda", generator=g)
+    R1 = torch.randn(n, k, dtype=torch.float64, device="cuda", generator=g)
+    R2 = torch.randn(n, m, dtype=torch.float64, device="cuda", generator=g)
+    out, res = {"n": n, "k": k, "m": m}, {}
+    for variant, name in ((1, "fma"), (2, "dmma")):  # CACG_GRAM_FMA, CACG_GRAM_DMMA
+        Cm = torch.empty(k, k + m, dtype=torch.float64, device="cuda")
+
+        def run():
+            rc = lib.cacg_k_gram(0, variant, n, L.data_ptr(), k, k, R1.data_ptr(), k, k,
+                                 R2.data_ptr(), m, m, Cm.data_ptr(), k + m, None)
+            assert rc == 0, rc
+
+        run()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(5):
+            run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        out[name] = {"ms": ms, "tflops": 2.0 * n * k * (k + m) / (ms * 1e-3) / 1e12}
+        res[name] = Cm.clone()
+    out["max_rel_diff"] = float((res["fma"] - res["dmma"]).abs().max() / res["fma"].abs().max())
+    print(json.dumps(out))
+    return 0
+
+
 def run_config4_sweep():
     """The ill-conditioned configuration at its shape: 2-D variable-coefficient
     diffusion 1024^2 (log-normal sigma 1.5 edge conductivities, seed 3, +1e-6
@@ -638,13 +682,15 @@ def main():
     ap.add_argument("--serving-load", type=float, default=0.7)
     ap.add_argument("--spmm-format", choices=["auto", "csr"], default="auto",
                     help="csr: the headline solves use the CSR SpMM (profiling)")
-    ap.add_argument("--sweep", choices=["config4"], default=None,
+    ap.add_argument("--sweep", choices=["config4", "gram64"], default=None,
                     help="run a recorded sweep instead of the bench line")
     args = ap.parse_args()
     global SPMM_FORMAT
     SPMM_FORMAT = args.spmm_format
     if args.sweep == "config4":
         return run_config4_sweep()
+    if args.sweep == "gram64":
+        return run_gram64_sweep()
     w = WORKLOADS[args.workload]
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
