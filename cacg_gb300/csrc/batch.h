@@ -25,8 +25,8 @@ constexpr int kBThreads = 256;
 
 // Gram split-K: a block takes one piece of a request (bpiece rows), staged
 // through shared memory bgchunk rows at a time; the piece's sums stay in
-// registers (FP32 class: FP32 over the piece's 256 rows, the single-request
-// tensor-core Gram's group length) and are written as one FP64 partial.
+// registers (FP32 class: FP32 over the piece's 256 rows) and are written as
+// one FP64 partial.
 template <typename T>
 __host__ __device__ constexpr int bgchunk() {
     return sizeof(T) == 4 ? 64 : 32;

@@ -368,8 +368,8 @@ __global__ void __launch_bounds__(kBThreads) bk_residual(const BBatch *__restric
 // product, summed in registers over the whole piece; when the product has
 // few tiles, G row groups (rows i = g mod G) run side by side and their sums
 // are added in group order.  The piece sums in the operands' precision (FP64
-// class: FP64; FP32 class: FP32 over 256 rows, the single-request tensor-core
-// Gram's FP32 group); the piece partials are summed in FP64, piece by piece.
+// class: FP64; FP32 class: FP32 over the piece's 256 rows); the piece
+// partials are summed in FP64, piece by piece.
 __device__ __forceinline__ int bk_gram_groups(int ntiles) {
     int G = 1;
     while (G < 8 && ntiles * G * 2 <= kBThreads) G *= 2;

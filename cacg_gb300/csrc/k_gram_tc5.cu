@@ -9,9 +9,12 @@
 // into three bf16 slices (x = x1 + x2 + x3, round-to-nearest at each split)
 // and the six slice products of order <= 2^-16 are accumulated by tcgen05.mma
 // (kind::f16, bf16 inputs, FP32 accumulator in TMEM).  The FP32 accumulator
-// covers one group of 8 K-steps (256 rows); the group's tile is then read
-// from TMEM (tcgen05.ld) and added to float-float registers (TwoSum), one
-// accumulator row per thread, and converted to FP64 once at the end.  Per-CTA FP64 partials go to the split-K workspace and the
+// covers one group of kT5Flush = 2 K-steps (64 rows); the group's tile is
+// then read from TMEM (tcgen05.ld) and added to float-float registers
+// (TwoSum on packed FP32 pairs), one accumulator row per thread, and
+// converted to FP64 once at the end.  Groups of 64 rows rather than 256 cost
+// about 5 % more per Gram and take the 128^3, 16-RHS mixed solve from 32 to
+// 30 outer iterations (29 in FP64).  Per-CTA FP64 partials go to the split-K workspace and the
 // fixed-order reduction of k_gram.cu finishes the sum.
 //
 // Pipeline of one CTA (256 threads, one row chunk of the split-K, one output
@@ -48,7 +51,7 @@ namespace cacg {
 constexpr int kT5KT = 32;        // rows (K) per step: two K = 16 UMMAs per product
 constexpr int kT5M = 128;        // UMMA M (output rows = columns of L, zero-padded)
 constexpr int kT5Threads = 256;  // 8 warps
-constexpr int kT5Flush = 8;      // K-steps per FP32 accumulation group
+constexpr int kT5Flush = 2;      // K-steps (32 rows each) per FP32 accumulation group
 constexpr int kT5Stages = 4;     // FP32 ring depth
 constexpr int kT5MaxUnits = 4;   // (column, 8 rows) conversion units per thread per step
 constexpr int kT5MaxN = 128;     // output tile columns (UMMA N)
@@ -490,13 +493,10 @@ __global__ void __launch_bounds__(kT5wThreads, 1)
                 for (int c4 = 0; c4 < 4; ++c4) {
                     if (h0 + c4 >= NC8) break;
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const float v = __uint_as_float(r[c4][q]);
-                        float &hi = acc_hi[4 * (h0 + c4) + q];
-                        const float s = hi + v;
-                        const float bp = s - hi;
-                        acc_lo[4 * (h0 + c4) + q] += (hi - (s - bp)) + (v - bp);
-                        hi = s;
+                    for (int q = 0; q < 4; q += 2) {
+                        const int i = 4 * (h0 + c4) + q;
+                        t5_twosum2(acc_hi[i], acc_hi[i + 1], acc_lo[i], acc_lo[i + 1],
+                                   __uint_as_float(r[c4][q]), __uint_as_float(r[c4][q + 1]));
                     }
                 }
             }

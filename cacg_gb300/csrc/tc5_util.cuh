@@ -206,4 +206,29 @@ __device__ __forceinline__ void t5_split2(float x0, float x1, unsigned &hw, unsi
         : "f"(x0), "f"(x1));
 }
 
+// (hi, lo) += v on two lanes at once: TwoSum (Knuth) as packed FP32 pairs,
+// per lane s = hi + v; bp = s - hi; lo += (hi - (s - bp)) + (v - bp); hi = s,
+// each operation rounded to nearest as in the scalar sequence, so the pairs
+// equal the scalar results bit for bit (7 packed instructions for 2 values).
+__device__ __forceinline__ void t5_twosum2(float &h0, float &h1, float &l0, float &l1, float v0,
+                                           float v1) {
+    asm("{\n"
+        ".reg .b64 h, v, l, s, bp, t, e1, e2;\n"
+        "mov.b64 h, {%0, %1};\n"
+        "mov.b64 l, {%2, %3};\n"
+        "mov.b64 v, {%4, %5};\n"
+        "add.rn.f32x2 s, h, v;\n"
+        "sub.rn.f32x2 bp, s, h;\n"
+        "sub.rn.f32x2 t, s, bp;\n"
+        "sub.rn.f32x2 e1, h, t;\n"
+        "sub.rn.f32x2 e2, v, bp;\n"
+        "add.rn.f32x2 e1, e1, e2;\n"
+        "add.rn.f32x2 l, l, e1;\n"
+        "mov.b64 {%0, %1}, s;\n"
+        "mov.b64 {%2, %3}, l;\n"
+        "}\n"
+        : "+f"(h0), "+f"(h1), "+f"(l0), "+f"(l1)
+        : "f"(v0), "f"(v1));
+}
+
 }  // namespace cacg

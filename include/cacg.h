@@ -63,8 +63,8 @@ extern "C" {
 #define CACG_GRAM_TC_SLICES 4 /* same products, from bf16 slice planes written by the
                                  producers (cacg_k_gram splits its inputs first) */
 #define CACG_GRAM_TC5 5  /* same products on the 5th-generation tensor cores
-                            (tcgen05.mma, accumulator in tensor memory, float-float
-                            sums across 256-row groups) */
+                            (tcgen05.mma, accumulator in tensor memory, FP32 over
+                            64-row groups, float-float sums across groups) */
 
 #define CACG_ALG_CACG 0 /* s-step Chebyshev-basis CG: cbcg_v1 (m = 1) / bcbcg_v1 */
 #define CACG_ALG_BCG 1  /* block CG, bcg_v1 (src/bcgKernel.c:22) */
