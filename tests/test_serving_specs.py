@@ -29,3 +29,15 @@ def test_build_request_shapes():
     rp, ci, v, B = SV.build_request(sp)
     assert len(rp) == 6 ** 3 + 1 and B.shape == (216, 3)
     assert math.isclose(v[rp[0]:rp[1]].max(), 6.05)
+
+
+def test_command_line_help_and_size_cap():
+    import pytest
+
+    with pytest.raises(SystemExit) as e:
+        SV.main(["--help"])
+    assert e.value.code == 0
+    # --max-rows caps the stream's sizes (the batched engine's default limit)
+    specs = SV.request_specs(500, seed=4, nmax=65536)
+    n = np.array([s["N"] ** (2 if s["kind"] == "lap2d" else 3) for s in specs], float)
+    assert n.max() <= 65536 * 1.05
