@@ -870,8 +870,11 @@ int launch_dia_spmm(cudaStream_t st, const DevMatrix *A, int w, const T *X, int6
     if (vec)
         return launch_dia_kernel<T, kDiaR, VN>(st, A, vals, w, X, ldx, Y, ldy, Z1, ldz1, Z2,
                                                ldz2, ca, cb, cc);
-    return launch_dia_kernel<T, 1, 1>(st, A, vals, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2, ca, cb,
-                                      cc);
+    // unaligned blocks (a column slice of width m % 4 != 0, e.g. a basis
+    // step T_j inside the n x k basis): scalar columns, still 4 rows a thread
+    // with the values staged (the same FMAs in the same order as R = 1)
+    return launch_dia_kernel<T, kDiaR / 2, 1>(st, A, vals, w, X, ldx, Y, ldy, Z1, ldz1, Z2, ldz2,
+                                              ca, cb, cc);
 }
 
 template int launch_dia_spmm<float>(cudaStream_t, const DevMatrix *, int, const float *, int64_t,
