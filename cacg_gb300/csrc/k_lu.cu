@@ -141,6 +141,74 @@ __global__ void __cluster_dims__(kLucCtas, 1, 1) __launch_bounds__(kLucThreads)
     cluster.sync();  // no CTA leaves while another may still read its rows
 }
 
+// One CTA with one barrier per elimination step (k <= kLuLaMaxK): warp 0
+// updates row d + 1 at step d and at once takes its pivot and scales it into
+// U's row -- the next step's critical path -- while warps 1..7 update rows
+// d + 2 .. k - 1 as one flat range of (row, column) entries, so every FP64
+// instruction of the trailing update carries 32 useful lanes.  Every element
+// sees the same operations in the same order as lu_factor_kernel
+// (bit-identical factors); the two-barrier factor and the cluster factor pay
+// a barrier (a cluster barrier) and the serial pivot work at every step.
+constexpr int kLuLaThreads = 256;
+constexpr int kLuLaMaxK = 128;  // k x k doubles in shared memory (128 KB)
+
+__device__ __forceinline__ void lu_pivot_row(double *W, int k, int i, double *Dinv, int lane,
+                                             int &bad) {
+    double inv = 0.0;
+    if (lane == 0) {
+        const double piv = W[i * k + i];
+        if (piv == 0.0 || !isfinite(piv)) bad = 1;
+        inv = 1.0 / piv;
+        Dinv[i] = inv;
+    }
+    inv = __shfl_sync(0xffffffffu, inv, 0);
+    for (int c = i + 1 + lane; c < k; c += 32) W[i * k + c] *= inv;
+}
+
+__global__ void __launch_bounds__(kLuLaThreads)
+    lu_factor_la_kernel(int k, const double *__restrict__ M, double *__restrict__ F,
+                        int *__restrict__ status) {
+    extern __shared__ __align__(16) double lw[];
+    const int kk = k * k;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < kk; i += blockDim.x) lw[i] = M[i];
+    __syncthreads();
+    double *Dinv = F + (size_t)kk;
+    int bad = 0;
+    if (warp == 0) lu_pivot_row(lw, k, 0, Dinv, lane, bad);
+    __syncthreads();
+    for (int d = 0; d + 1 < k; ++d) {
+        const int x = k - d - 1;  // trailing columns d + 1 .. k - 1
+        const double *U = lw + (size_t)d * k;
+        if (warp == 0) {
+            double *wr = lw + (size_t)(d + 1) * k;
+            const double lid = wr[d];
+            for (int c = d + 1 + lane; c < k; c += 32) wr[c] = wr[c] - lid * U[c];
+            __syncwarp();
+            lu_pivot_row(lw, k, d + 1, Dinv, lane, bad);
+        } else {
+            // entry e = q x + r of rows d + 2 .. k - 1: row d + 2 + q, column
+            // d + 1 + r; q = floor(e / x) as the high word of e * ceil(2^32 / x)
+            // (exact for e < 2^32 / x)
+            const uint32_t mg = x > 1 ? 0xFFFFFFFFu / (uint32_t)x + 1u : 0u;
+            for (int e = tid - 32; e < (x - 1) * x; e += kLuLaThreads - 32) {
+                const int q = x > 1 ? (int)__umulhi((uint32_t)e, mg) : e;
+                double *wr = lw + (size_t)(d + 2 + q) * k;
+                const int c = d + 1 + (e - q * x);
+                wr[c] = wr[c] - wr[d] * U[c];
+            }
+        }
+        __syncthreads();
+    }
+    double *FT = F + (size_t)kk + k;
+    for (int idx = tid; idx < kk; idx += blockDim.x) {
+        const int i = idx / k, j = idx - i * k;
+        F[idx] = lw[idx];
+        FT[idx] = lw[(size_t)j * k + i];
+    }
+    if (bad && status) atomicOr(status, kStatusBreakdown);
+}
+
 // Y (k x r) from the factor F (k*k factors + k reciprocal diagonal) and RHS
 // (k x r).  Each CTA solves kLuRC columns with kLuTPC threads per column
 // splitting the inner products; many CTAs spread the FP64 work over SMs.
@@ -282,6 +350,12 @@ static int launch_sweep(cudaStream_t st, int k, const double *F, int r, const do
 
 int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *status) {
     if (k <= 0) return CACG_ERR_ARG;
+    if (k <= kLuLaMaxK) {
+        const size_t smem = (size_t)k * k * sizeof(double);
+        set_smem_attr(lu_factor_la_kernel, kLuLaMaxK * kLuLaMaxK * (int)sizeof(double));
+        lu_factor_la_kernel<<<1, kLuLaThreads, smem, st>>>(k, M, F, status);
+        return check_launch();
+    }
     if (k >= kLucCtas && k <= kLucMaxK) {
         const size_t csmem = ((size_t)((k + kLucCtas - 1) / kLucCtas) * k + k) * sizeof(double);
         set_smem_attr(lu_factor_cluster_kernel, (int)(((size_t)(kLucMaxK / kLucCtas) * kLucMaxK + kLucMaxK) * sizeof(double)));
