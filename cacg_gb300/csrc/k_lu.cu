@@ -150,7 +150,7 @@ __global__ void __cluster_dims__(kLucCtas, 1, 1) __launch_bounds__(kLucThreads)
 // (bit-identical factors); the two-barrier factor and the cluster factor pay
 // a barrier (a cluster barrier) and the serial pivot work at every step.
 constexpr int kLuLaThreads = 256;
-constexpr int kLuLaMaxK = 128;  // k x k doubles in shared memory (128 KB)
+constexpr int kLuLaMaxK = 128;  // k x k doubles in shared memory (128 KB); taken for k <= 64
 
 __device__ __forceinline__ void lu_pivot_row(double *W, int k, int i, double *Dinv, int lane,
                                              int &bad) {
@@ -350,7 +350,9 @@ static int launch_sweep(cudaStream_t st, int k, const double *F, int r, const do
 
 int launch_lu_factor(cudaStream_t st, int k, const double *M, double *F, int *status) {
     if (k <= 0) return CACG_ERR_ARG;
-    if (k <= kLuLaMaxK) {
+    // k <= 64 (the serving stream's shapes): one CTA; larger k: the cluster
+    // (at k = 96 it measured 8 % less LU time per outer iteration)
+    if (k <= 64) {
         const size_t smem = (size_t)k * k * sizeof(double);
         set_smem_attr(lu_factor_la_kernel, kLuLaMaxK * kLuLaMaxK * (int)sizeof(double));
         lu_factor_la_kernel<<<1, kLuLaThreads, smem, st>>>(k, M, F, status);
