@@ -194,6 +194,10 @@ int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl
                 bool symmetric = false);
 size_t gram_workspace_bytes(int64_t n, int ka, int kb);
 
+// dst = src for an n x w FP32 block (rows of lds / ldd values)
+int launch_copy_rows_f32(cudaStream_t st, int64_t n, int w, const float *src, int64_t lds,
+                         float *dst, int64_t ldd);
+
 // Tensor-core Gram of FP32 blocks (three bf16 slices per value, six slice
 // products, FP32 accumulation over 256-row groups, FP64 across groups).
 int launch_gram_tc(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int ka,

@@ -325,7 +325,7 @@ constexpr int kRedElems = 64;  // output elements per block (x 4 quarters = 256 
 __global__ void __launch_bounds__(4 * kRedElems)
     gram_reduce_kernel(const double *__restrict__ part, int nchunks, int ntiles, int BA, int BB,
                        int tilesB, int ka, int kb, int kb1, double *__restrict__ C1, int ldc1,
-                       double *__restrict__ C2, int ldc2, int sym) {
+                       double *__restrict__ C2, int ldc2, int sym, int gap = 0) {
     __shared__ double qs[4][kRedElems];
     const int el = threadIdx.x % kRedElems, q = threadIdx.x / kRedElems;
     const int idx = blockIdx.x * kRedElems + el;
@@ -333,7 +333,9 @@ __global__ void __launch_bounds__(4 * kRedElems)
     const int a = active ? idx / kb : 0, b = active ? idx % kb : 0;
     // symmetric leading block: the lower triangle reads its mirror image
     const bool mirror = sym && b < kb1 && a > b;
-    const int pa = mirror ? b : a, pb = mirror ? a : b;
+    // gap: the partial tiles hold `gap` zero columns between the R1 and R2
+    // parts (an R1 width padded to the tensor-core kernel's 8-column units)
+    const int pa = mirror ? b : a, pb = mirror ? a : (b < kb1 ? b : b + gap);
     const int tile = (pa / BA) * tilesB + (pb / BB);
     const size_t off = (size_t)tile * BA * BB + (size_t)(pa % BA) * BB + (pb % BB);
     const size_t stride = (size_t)ntiles * BA * BB;
@@ -477,10 +479,10 @@ int launch_gram(cudaStream_t st, int variant, int64_t n, const T *L, int64_t ldl
 
 int launch_gram_reduce(cudaStream_t st, const double *part, int nchunks, int ntiles, int BA,
                        int BB, int tilesB, int ka, int kb, int kb1, double *C1, int ldc1,
-                       double *C2, int ldc2) {
+                       double *C2, int ldc2, int gap) {
     int tot = ka * kb;
     gram_reduce_kernel<<<(tot + kRedElems - 1) / kRedElems, 4 * kRedElems, 0, st>>>(
-        part, nchunks, ntiles, BA, BB, tilesB, ka, kb, kb1, C1, ldc1, C2, ldc2, 0);
+        part, nchunks, ntiles, BA, BB, tilesB, ka, kb, kb1, C1, ldc1, C2, ldc2, 0, gap);
     return check_launch();
 }
 

@@ -322,7 +322,7 @@ size_t gram_tc_workspace_bytes(int64_t n, int ka, int kb) {
 // the fixed-order reduction kernel of k_gram.cu
 int launch_gram_reduce(cudaStream_t st, const double *part, int nchunks, int ntiles, int BA,
                        int BB, int tilesB, int ka, int kb, int kb1, double *C1, int ldc1,
-                       double *C2, int ldc2);
+                       double *C2, int ldc2, int gap = 0);
 
 int launch_gram_tc(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int ka,
                    const float *R1, int64_t ldr1, int kb1, const float *R2, int64_t ldr2, int kb2,

@@ -698,8 +698,11 @@ static T5Plan plan_tc5(int64_t n, int ka, int kb) {
 }
 
 size_t gram_tc5_workspace_bytes(int64_t n, int ka, int kb) {
-    T5Plan p = plan_tc5(n, ka, kb);
-    return (size_t)p.nchunks * p.tilesA * p.tilesB * p.BA * p.BB * sizeof(double);
+    // also the plan of an R1 part padded by 4 columns (see launch_gram_tc5)
+    T5Plan p = plan_tc5(n, ka, kb), pp = plan_tc5(n, ka, kb + 4);
+    return std::max((size_t)p.nchunks * p.tilesA * p.tilesB * p.BA * p.BB,
+                    (size_t)pp.nchunks * pp.tilesA * pp.tilesB * pp.BA * pp.BB) *
+           sizeof(double);
 }
 
 bool gram_tc5_supported(int ka, int kb) {
@@ -715,7 +718,7 @@ static void t5_set_attr() {
 
 int launch_gram_reduce(cudaStream_t st, const double *part, int nchunks, int ntiles, int BA,
                        int BB, int tilesB, int ka, int kb, int kb1, double *C1, int ldc1,
-                       double *C2, int ldc2);
+                       double *C2, int ldc2, int gap = 0);
 
 template <int NC8>
 static void t5m_set_attr() {
@@ -725,19 +728,22 @@ static void t5m_set_attr() {
 // The MN-major / TMA kernel; CACG_ERR_UNSUPPORTED when the operands do not
 // allow TMA boxes (16-byte aligned bases and row strides; an R1/R2 boundary
 // on an 8-column octet) or the ring does not fit.
+// kb1map <= kb1: R1's true width; columns [kb1map, kb1) of the kernel's R1
+// part read as zeros (outside the tensor map), so an R1 width of 4 mod 8 can
+// be padded to the converters' 8-column units.
 static int launch_tc5m(cudaStream_t st, const T5Plan &p, int64_t n, const float *L, int64_t ldl,
                        int ka, const float *R1, int64_t ldr1, int kb1, const float *R2,
-                       int64_t ldr2, int kb2, double *ws, int *status) {
+                       int64_t ldr2, int kb2, double *ws, int *status, int kb1map) {
     if (n <= 0 || n >= (1ll << 31) - 4096) return CACG_ERR_UNSUPPORTED;
     if (ldl % 4 || ldr1 % 4 || (kb2 > 0 && (ldr2 % 4 || kb1 % 8)) || !aligned16(L) ||
-        !aligned16(R1) || (kb2 > 0 && !aligned16(R2)))
+        !aligned16(R1) || (kb2 > 0 && !aligned16(R2)) || kb1map > kb1 || kb1map <= 0)
         return CACG_ERR_UNSUPPORTED;
     const CUtensorMapSwizzle sw = CU_TENSOR_MAP_SWIZZLE_128B;
     const CUtensorMapL2promotion pr = CU_TENSOR_MAP_L2_PROMOTION_L2_256B;
     CUtensorMap tmL, tmR1, tmR2;
     if (!tma_encode_2d(&tmL, L, (uint64_t)ka, (uint64_t)n, (uint64_t)ldl * 4, kT5mBox, kT5mBox,
                        sw, pr) ||
-        !tma_encode_2d(&tmR1, R1, (uint64_t)kb1, (uint64_t)n, (uint64_t)ldr1 * 4, kT5mBox,
+        !tma_encode_2d(&tmR1, R1, (uint64_t)kb1map, (uint64_t)n, (uint64_t)ldr1 * 4, kT5mBox,
                        kT5mBox, sw, pr))
         return CACG_ERR_UNSUPPORTED;
     if (kb2 > 0) {
@@ -793,7 +799,25 @@ int launch_gram_tc5(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int
     T5Plan p = plan_tc5(n, ka, kb);
     const size_t need = (size_t)p.nchunks * p.tilesA * p.tilesB * p.BA * p.BB * sizeof(double);
     if (!ws || need > ws_bytes) return CACG_ERR_ARG;
-    int mrc = launch_tc5m(st, p, n, L, ldl, ka, R1, ldr1, kb1, R2, ldr2, kb2, ws, status);
+    // Q^T [AQ | R] with k = 4 mod 8 (k = 4m, m odd): the TMA kernel's R1 part
+    // padded by 4 zero columns, the reduction skipping them
+    int gap = 0;
+    int mrc = CACG_ERR_UNSUPPORTED;
+    if (kb2 > 0 && kb1 % 8 == 4) {
+        const int kb1p = kb1 + 4;
+        T5Plan pp = plan_tc5(n, ka, kb1p + kb2);
+        const size_t needp =
+            (size_t)pp.nchunks * pp.tilesA * pp.tilesB * pp.BA * pp.BB * sizeof(double);
+        if (needp <= ws_bytes) {
+            mrc = launch_tc5m(st, pp, n, L, ldl, ka, R1, ldr1, kb1p, R2, ldr2, kb2, ws, status, kb1);
+            if (mrc != CACG_ERR_UNSUPPORTED) {
+                if (mrc != CACG_OK) return mrc;
+                return launch_gram_reduce(st, ws, pp.nchunks, pp.tilesA * pp.tilesB, pp.BA, pp.BB,
+                                          pp.tilesB, ka, kb, kb1, C1, ldc1, C2, ldc2, 4);
+            }
+        }
+    }
+    mrc = launch_tc5m(st, p, n, L, ldl, ka, R1, ldr1, kb1, R2, ldr2, kb2, ws, status, kb1);
     if (mrc != CACG_ERR_UNSUPPORTED) {
         if (mrc != CACG_OK) return mrc;
     } else if (n > 0) {
@@ -828,7 +852,7 @@ int launch_gram_tc5(cudaStream_t st, int64_t n, const float *L, int64_t ldl, int
         if (cudaMemsetAsync(ws, 0, need, st) != cudaSuccess) return CACG_ERR_CUDA;
     }
     return launch_gram_reduce(st, ws, n > 0 ? p.nchunks : 1, p.tilesA * p.tilesB, p.BA, p.BB,
-                              p.tilesB, ka, kb, kb1, C1, ldc1, C2, ldc2);
+                              p.tilesB, ka, kb, kb1, C1, ldc1, C2, ldc2, gap);
 }
 
 }  // namespace cacg

@@ -642,6 +642,27 @@ int launch_xrupdate_direct(cudaStream_t st, int64_t n, int k, int m, const T *Q,
     return launch_colsum(st, ws, (int)blocks, m, norms);
 }
 
+// dst = src for an n x w FP32 block, rows of lds and ldd values
+__global__ void copy_rows_f32_kernel(int64_t n, int w, const float *__restrict__ src, int64_t lds,
+                                     float *__restrict__ dst, int64_t ldd) {
+    const int64_t total = n * w;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / w;
+        const int c = (int)(e - r * w);
+        dst[r * ldd + c] = src[r * lds + c];
+    }
+}
+
+int launch_copy_rows_f32(cudaStream_t st, int64_t n, int w, const float *src, int64_t lds,
+                         float *dst, int64_t ldd) {
+    if (n <= 0 || w <= 0) return CACG_OK;
+    const int64_t blocks =
+        std::min<int64_t>((n * w + 255) / 256, (int64_t)sm_count() * 16);
+    copy_rows_f32_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, w, src, lds, dst, ldd);
+    return check_launch();
+}
+
 // ------------------------------------------------------ residual epilogue
 // After R = B - A X (launch_spmm): S0 = cast(R), R32 = (float)R, norm partials.
 template <typename T>

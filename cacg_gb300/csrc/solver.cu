@@ -161,8 +161,8 @@ void DevMatrix::release() {
 static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct Layout {
-    size_t S, Q, AQ, R, R32, Xff, Rff, Bnorm, small, gram, norm, lanczos, total;
-    size_t o_S, o_Q, o_AQ, o_R, o_R32, o_Xff, o_Rff, o_small, o_gram, o_norm, o_lanczos;
+    size_t S, Q, AQ, R, R32, R32p, Xff, Rff, Bnorm, small, gram, norm, lanczos, total;
+    size_t o_S, o_Q, o_AQ, o_R, o_R32, o_R32p, o_Xff, o_Rff, o_small, o_gram, o_norm, o_lanczos;
     size_t Ssl, R32sl, o_Ssl, o_Qsl, o_AQsl, o_R32sl;
     bool slices;
 };
@@ -184,6 +184,11 @@ static Layout layout(int64_t n, int m, int s, int prec, bool lanczos, bool slice
     L.S = L.Q = L.AQ = align256((size_t)n * k * es + 64);
     L.R = align256((size_t)n * m * 8);
     L.R32 = prec == CACG_MIXED ? align256((size_t)n * m * 4) : 0;
+    // R32 again with its rows padded to 16 bytes, for the TMA-fed Gram when m
+    // is not a multiple of 4 (R32's own rows are m values)
+    L.R32p = prec == CACG_MIXED && m % 4 != 0 && k % 4 == 0
+                 ? align256((size_t)n * (size_t)((m + 3) & ~3) * 4)
+                 : 0;
     L.Xff = prec == CACG_MIXED ? align256((size_t)n * m * 8) : 0;  // X as FP32 hi, lo
     L.Rff = prec == CACG_MIXED ? align256((size_t)n * m * 8) : 0;  // R as FP32 hi, lo
     L.Ssl = slices ? align256((size_t)3 * n * k * 2) : 0;
@@ -206,6 +211,7 @@ static Layout layout(int64_t n, int m, int s, int prec, bool lanczos, bool slice
     L.o_AQ = o; o += L.AQ;
     L.o_R = o; o += L.R;
     L.o_R32 = o; o += L.R32;
+    L.o_R32p = o; o += L.R32p;
     L.o_Xff = o; o += L.Xff;
     L.o_Rff = o; o += L.Rff;
     L.o_small = o; o += L.small;
@@ -450,6 +456,8 @@ struct SolveBuffers {
     void *S, *Q, *AQ;
     double *R;
     float *R32;
+    float *R32p;  // R32 with rows of ldr32p >= m values (nullptr: not needed)
+    int ldr32p;
     double *QtAS, *QtAQ, *QtR, *F, *alpha, *beta, *norms, *bnorm, *tnorm, *bounds, *scal;
     int *status;
     double *gram_ws;
@@ -468,6 +476,8 @@ static void carve(char *base, const Layout &L, int m, int k, SolveBuffers *b) {
     b->AQ = base + L.o_AQ;
     b->R = (double *)(base + L.o_R);
     b->R32 = L.R32 ? (float *)(base + L.o_R32) : nullptr;
+    b->R32p = L.R32p ? (float *)(base + L.o_R32p) : nullptr;
+    b->ldr32p = (m + 3) & ~3;
     b->Xff = L.Xff ? (float *)(base + L.o_Xff) : nullptr;
     b->Rff = L.Rff ? (float *)(base + L.o_Rff) : nullptr;
     double *sm = (double *)(base + L.o_small);
@@ -813,12 +823,27 @@ struct Solver {
         if (rc) return rc;
         const T *Rp = prec == CACG_MIXED ? (const T *)(const void *)b.R32
                                          : (const T *)(const void *)b.R;
+        int64_t ldrp = m;
         prof.begin(CACG_PHASE_GRAM, dn * (2.0 * k + m) * ees, 2.0 * dn * k * (k + m));
+        if constexpr (std::is_same<T, float>::value) {
+            // rows of m % 4 != 0 FP32 values are not 16-byte aligned: a padded
+            // copy lets the Gram take TMA boxes (the tensor-map width stays m)
+            if (!slices && b.R32p && gram_tc5_supported(k, k + m) &&
+                (p.gram_variant == CACG_GRAM_AUTO || p.gram_variant == CACG_GRAM_TC5)) {
+                rc = launch_copy_rows_f32(st, n, m, b.R32, m, b.R32p, b.ldr32p);
+                if (rc) {
+                    prof.end();
+                    return rc;
+                }
+                Rp = b.R32p;
+                ldrp = b.ldr32p;
+            }
+        }
         if (slices)
             rc = launch_gram_tcs(st, n, b.Qsl, k, k, b.AQsl, k, k, b.R32sl, m, m, b.QtAQ, k,
                                  b.QtR, m, b.gram_ws, b.gram_ws_bytes);
         else
-            rc = gram<T>(Q, k, AQ, k, k, Rp, m, m, b.QtAQ, k, b.QtR, m, true);
+            rc = gram<T>(Q, k, AQ, k, k, Rp, ldrp, m, b.QtAQ, k, b.QtR, m, true);
         prof.end();
         if (rc) return rc;
         prof.begin(CACG_PHASE_LU, 16.0 * k * k, (2.0 / 3.0) * k * k * k + 2.0 * k * k * m);
