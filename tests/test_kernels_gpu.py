@@ -448,8 +448,9 @@ def test_gerschgorin_exact(lib, torch_cuda, kind, N):
                                           (20000, 160, 160, 16)])
 def test_gram_tensor_core_bf16_slices(lib, torch_cuda, variant, n, ka, kb1, kb2):
     """FP32 inputs on the bf16 tensor cores (three slices, six products,
-    FP32 over 256-row groups, FP64 across): normwise within 4e-6 of the exact
-    FP64 Gram of the FP32 values (FP32 accumulation inside the tensor core)."""
+    FP32 over 256-row (mma.sync) or 64-row (tcgen05) groups, FP64 across):
+    normwise within 4e-6 of the exact FP64 Gram of the FP32 values (FP32
+    accumulation inside the tensor core)."""
     torch = torch_cuda
     if variant == 4 and (ka % 8 or kb1 % 8 or kb2 % 8):
         pytest.skip("slice planes need widths that are multiples of 8")
@@ -481,6 +482,27 @@ def test_gram_tc5_padded_rows_partial_chunks(lib, torch_cuda, n):
     C = torch.zeros((6, 7), dtype=torch.float64, device="cuda")
     rc = lib.cacg_k_gram(F32, 5, n, ptr(d["L"]), 8, 6, ptr(d["R1"]), 8, 4, ptr(d["R2"]), 4, 3,
                          ptr(C), 7, None)
+    assert rc == 0
+    assert relerr(host(C), want) <= 4e-6
+
+
+@pytest.mark.parametrize("ka,kw2,kb2", [(12, 4, 3), (20, 8, 5), (36, 4, 1)])
+@pytest.mark.parametrize("n", [29, 65537])
+def test_gram_tc5_tma_r1_width_4_mod_8(lib, torch_cuda, n, ka, kw2, kb2):
+    """tcgen05 Gram Q^T [AQ | R] with the AQ part 4 columns past a multiple of
+    8 (k = 4m, m odd) and R's rows 16-byte aligned (R = kb2 of kw2 columns):
+    the TMA kernel takes AQ widened by 4 zero columns outside its tensor map
+    and the reduction skips them."""
+    torch = torch_cuda
+    L = O.gen_rhs("normal", n, ka, 31).astype(np.float32)
+    R1 = O.gen_rhs("normal", n, ka, 32).astype(np.float32)
+    R2w = O.gen_rhs("normal", n, kw2, 33).astype(np.float32)
+    want = O.port_gram(L.astype(np.float64),
+                       np.hstack([R1, R2w[:, :kb2]]).astype(np.float64))
+    d = {k_: dev(torch, a) for k_, a in dict(L=L, R1=R1, R2=R2w).items()}
+    C = torch.zeros((ka, ka + kb2), dtype=torch.float64, device="cuda")
+    rc = lib.cacg_k_gram(F32, 5, n, ptr(d["L"]), ka, ka, ptr(d["R1"]), ka, ka, ptr(d["R2"]), kw2,
+                         kb2, ptr(C), ka + kb2, None)
     assert rc == 0
     assert relerr(host(C), want) <= 4e-6
 
