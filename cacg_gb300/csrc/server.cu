@@ -260,7 +260,7 @@ struct BSlot {
     double *gws = nullptr;
     double bn[kBMaxM];
     int since_rr = 0;
-    bool resid = false;        // in this round's residual launch
+    bool resid = false;        // in the next residual launch
     bool r_true = false;       // R holds B - A X for the current X
     bool done = false;
     int final_status = CACG_OK;
@@ -490,7 +490,7 @@ struct Engine {
     }
 
     // residual launch for the slots with s.resid set; norms to h_norms
-    int residual_round() {
+    int residual_pass() {
         bool any = false;
         for (int c = 0; c < 2; ++c) {
             bool anyc = false;
@@ -658,7 +658,7 @@ struct Engine {
                 hb[2 * i + 1] = p.lambda_max;
             }
         }
-        int rc = residual_round();  // synchronises the stream
+        int rc = residual_pass();  // synchronises the stream
         if (rc) return rc;
         for (size_t i = 0; i < added.size(); ++i) {
             BSlot &s = *added[i];
@@ -747,7 +747,7 @@ struct Engine {
         for (int c = 0; c < 2; ++c)
             for (auto &s : slots[c]) any = any || s->resid;
         if (!any) return CACG_OK;
-        int rc = residual_round();
+        int rc = residual_pass();
         if (rc) return rc;
         for (int c = 0; c < 2; ++c) {
             for (size_t i = 0; i < slots[c].size(); ++i) {
@@ -786,7 +786,7 @@ struct Engine {
                     s->resid = !s->r_true;
                 }
         if (!any) return CACG_OK;
-        int rc = residual_round();
+        int rc = residual_pass();
         if (rc) return rc;
         std::vector<std::unique_ptr<BSlot>> out;
         for (int c = 0; c < 2; ++c) {
